@@ -1,0 +1,354 @@
+"""Benchmark of the fused LBM step (MLUPS and fraction of the HBM roofline).
+
+Default workload: lid-driven cavity, D3Q19, recursive-regularised collision, FP32
+populations, 256^3 cells (the size the roofline target is stated at), lattice units
+nu = 0.032, lid u = 0.05; synthetic data (the reference publishes no data set).
+A "step" is one LBM time step over the whole lattice (k_bulk + k_special).
+
+value  : device-resident throughput, MLUPS = cells * steps / time (CUDA events on the
+         library's stream, max over ranks).
+e2e    : the same metric through the C ABI with host buffers: every e2e step uploads the
+         populations from pinned host memory, runs E2E_INNER time steps and downloads the
+         populations (what the reference driver's restart/VTK cadence does), MLUPS counted
+         over the inner steps.
+roofline: k_bulk, algorithmic bytes = 152 B (D3Q19 FP32) per updated cell, divided by its
+         average launch time from CUDA events; peak = measured HBM copy bandwidth.
+variants: the FP16-shifted storage and the D3Q27 lattice on the same grid, and the
+         1024x256x4 cylinder-channel configuration, measured the same way.
+
+Multi-GPU: the step does not shard (one lattice per GPU, no halo exchange); under torchrun
+each rank runs an independent replica (weak scaling) and rank 0 reports the aggregate.
+
+--impl reference: the reference's own k_streamingCollision compiled as C (oracle/_ref) on
+all host cores, same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL = {(19, "fp32"): 152, (19, "fp16s"): 76, (19, "bf16s"): 76, (27, "fp32"): 216, (27, "fp16s"): 108,
+                  (27, "bf16s"): 108}
+E2E_INNER = 100
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_workload(name):
+    from lbffs_gb300 import case as K
+    from lbffs_gb300 import geometry as G
+    if name == "cavity256":
+        n = 256
+        c = K.make_case(n, n, n, 19, K.cavity_faces(0.05), nu=0.032)
+        return c, dict(collision="rr", sgs="smag", wall="bb", les=0.0)
+    if name == "cavity256_q27":
+        n = 256
+        c = K.make_case(n, n, n, 27, K.cavity_faces(0.05), nu=0.032)
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=0.0)
+    if name == "cylinder1024":
+        rng = np.random.default_rng(1)
+        cy = 128 + rng.uniform(-0.5, 0.5)
+        solid, sdf = G.cylinder_z(1024, 256, 4, 256.0, cy, 20.0)
+        c = K.make_case(1024, 256, 4, 19, K.channel_faces(0.05), nu=0.02, solid=solid, sdf=sdf)
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=0.0)
+    raise KeyError(name)
+
+
+def describe(name, storage):
+    return {"cavity256": f"lid-driven cavity D3Q19 RR {storage.upper()} 256^3, nu=0.032, lid 0.05 (synthetic)",
+            "cavity256_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256^3 (synthetic)",
+            "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)"}[name]
+
+
+def run_device(name, storage, steps, warmup, device, timing_pass=True):
+    import torch
+    import lbffs_gb300 as L
+    c, sel = make_workload(name)
+    lat = L.Lattice(c.nx, c.ny, c.nz, q=c.q, storage=storage, collision=sel["collision"], sgs=sel["sgs"],
+                    wall=sel["wall"], device=device)
+    lat.load_case(c)
+    stream = torch.cuda.ExternalStream(lat.stream(), device=device)
+    lat.step(warmup, les=sel["les"], store_fields=0)
+    lat.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if torch.distributed.is_initialized():
+        torch.distributed.barrier()
+    torch.cuda.synchronize(device)
+    e0.record(stream)
+    lat.step(steps, les=sel["les"], store_fields=0)
+    e1.record(stream)
+    e1.synchronize()
+    lat.synchronize()
+    torch.cuda.synchronize(device)
+    ms = e0.elapsed_time(e1)
+    counts = lat.cell_counts()
+    out = {"ms_per_step": ms / steps, "cells": c.elements, "fluid": counts["fluid"], "special": counts["special"],
+           "launches_per_step": 2 if counts["special"] > 0 else 1, "lat": lat, "case": c, "sel": sel}
+    if timing_pass:
+        lat.set_timing(True)
+        lat.step(steps, les=sel["les"], store_fields=0)
+        bulk_ms, n = lat.kernel_time("bulk")
+        sp_ms, nsp = lat.kernel_time("special")
+        lat.set_timing(False)
+        out["bulk_ms"] = bulk_ms / max(n, 1)
+        out["special_ms"] = sp_ms / max(nsp, 1)
+    return out
+
+
+def run_e2e(res, steps, device):
+    """Upload from pinned host memory, E2E_INNER steps, download: timed with CUDA events, the copies inside."""
+    import torch
+    lat, c, sel = res["lat"], res["case"], res["sel"]
+    host_in = torch.from_numpy(c.f).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    stream = torch.cuda.ExternalStream(lat.stream(), device=device)
+    import ctypes as C
+    lib = lat.lib
+
+    def one():
+        rc = lib.lbffs_upload(lat.h, 0, C.c_void_p(host_in.data_ptr()), host_in.numel() * 4)
+        assert rc == 0, lib.lbffs_last_error(lat.h)
+        lat.step(E2E_INNER, les=sel["les"], store_fields=0)
+        rc = lib.lbffs_download(lat.h, 0, C.c_void_p(host_out.data_ptr()), host_out.numel() * 4)
+        assert rc == 0, lib.lbffs_last_error(lat.h)
+
+    one()
+    n_e2e = max(1, min(steps, 3))
+    torch.cuda.synchronize(device)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(n_e2e):
+        one()
+    e1.record(stream)
+    e1.synchronize()
+    wall = time.perf_counter() - t0
+    ms = max(e0.elapsed_time(e1), wall * 1e3)
+    mlups = c.elements * E2E_INNER * n_e2e / (ms * 1e-3) / 1e6
+    return {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": int(host_in.numel() * 4),
+            "d2h_bytes_per_step": int(host_out.numel() * 4), "inner_steps": E2E_INNER, "e2e_steps": n_e2e,
+            "ms_per_e2e_step": ms / n_e2e}
+
+
+def cpu_reference_mlups(nx, ny, nz, steps, threads=0, kind_pref="reference"):
+    """The reference kernel compiled as C (oracle/_ref) or the CPU oracle, all host threads."""
+    from lbffs_gb300 import case as K
+    from oracle import ref as R
+    c = K.make_case(nx, ny, nz, 19, K.cavity_faces(0.05), nu=0.032)
+    kind = "reference" if (kind_pref == "reference" and R.available(19, "smag", "bb", "f32")) else "port"
+    solver = R.RefSolver(c, real="f32", nthreads=threads) if kind == "reference" else \
+        R.OracleSolver(c, real="f32", nthreads=threads)
+    solver.step(1)
+    t0 = time.perf_counter()
+    solver.step(steps)
+    dt = time.perf_counter() - t0
+    return c.elements * steps / dt / 1e6, kind, (threads or os.cpu_count())
+
+
+def traffic_from_profile():
+    """Per-launch DRAM bytes of k_bulk from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "k_bulk_d3q19_fp32_cavity.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch_256:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cavity256")
+    ap.add_argument("--storage", default="fp32")
+    ap.add_argument("--no-variants", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from oracle.build import build_oracle
+        build_oracle()
+        n = 256
+        # all host threads, the full workload; each step is one reference NDRange launch over 256^3 cells
+        from lbffs_gb300 import case as K
+        from oracle import ref as R
+        c = K.make_case(n, n, n, 19, K.cavity_faces(0.05), nu=0.032)
+        kind = "reference" if R.available(19, "smag", "bb", "f32") else "port"
+        solver = R.RefSolver(c, real="f32") if kind == "reference" else R.OracleSolver(c, real="f32")
+        solver.step(args.warmup)
+        t0 = time.perf_counter()
+        solver.step(args.steps)
+        dt = time.perf_counter() - t0
+        mlups = c.elements * args.steps / dt / 1e6
+        line = {"impl": "reference", "metric": "MLUPS", "value": mlups, "unit": "MLUPS", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": {"workload": describe("cavity256", "fp32"), "cells": c.elements},
+                "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": os.cpu_count(), "kind": kind,
+                                 "sample": f"256^3 cavity, {args.steps} steps (the full workload)"},
+                "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+
+    with ClockSampler(device) as clk:
+        res = run_device(args.workload, args.storage, args.steps, args.warmup, device)
+    clocks = clk.summary()
+    ms = res["ms_per_step"]
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    mlups = world * res["cells"] / (ms * 1e-3) / 1e6
+    e2e = run_e2e(res, args.steps, device)
+    if world > 1:
+        t = torch.tensor([e2e["value"]], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MIN)
+        e2e["value"] = float(t.item()) * world
+
+    q = res["case"].q
+    bpc = BYTES_PER_CELL[(q, args.storage)]
+    peak, peak_kind = peaks()
+    n_bulk = res["fluid"] - res["special"]
+    achieved = bpc * n_bulk / (res["bulk_ms"] * 1e-3) / 1e9
+    traffic = traffic_from_profile() if (args.workload == "cavity256" and args.storage == "fp32") else None
+
+    variants = {}
+    if rank == 0 and not args.no_variants and args.workload == "cavity256":
+        for vname, vst in (("cavity256", "fp16s"), ("cavity256", "bf16s"), ("cavity256_q27", "fp32"),
+                           ("cavity256_q27", "fp16s"), ("cylinder1024", "fp32"), ("cylinder1024", "fp16s")):
+            try:
+                r = run_device(vname, vst, args.steps, args.warmup, device)
+                vq = r["case"].q
+                vb = BYTES_PER_CELL[(vq, vst)]
+                vn = r["fluid"] - r["special"]
+                variants[f"{vname}_{vst}"] = {
+                    "workload": describe(vname, vst), "MLUPS": r["cells"] / (r["ms_per_step"] * 1e-3) / 1e6,
+                    "ms_per_step": r["ms_per_step"], "bulk_ms": r["bulk_ms"], "special_ms": r["special_ms"],
+                    "bulk_GBps": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9,
+                    "bulk_frac_of_peak": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9 / peak,
+                    "bytes_per_cell": vb}
+                r["lat"].close()
+                del r
+            except Exception as ex:  # a failing variant must not hide the headline
+                variants[f"{vname}_{vst}"] = {"error": str(ex)[:200]}
+
+    cpu = None
+    if rank == 0:
+        try:
+            cm, kind, cores = cpu_reference_mlups(128, 128, 128, 60)
+            cpu = {"value": cm, "unit": "MLUPS", "cores": cores, "kind": kind,
+                   "sample": "128^3 lid-driven cavity D3Q19 FP32, 60 steps, all host threads"}
+        except Exception as ex:
+            cpu = {"value": None, "unit": "MLUPS", "cores": os.cpu_count(), "kind": "reference",
+                   "sample": f"unavailable: {str(ex)[:120]}"}
+
+    if rank == 0:
+        line = {
+            "metric": "MLUPS", "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.storage == "fp32" else f"f32 compute, {args.storage} storage",
+            "data": "synthetic",
+            "config": {"workload": describe(args.workload, args.storage), "cells": res["cells"],
+                       "lattice": f"D3Q{q}", "storage": args.storage, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (populations %.2f GB per copy)" % (q * res["cells"] * bpc / 2 / q / 1e9)},
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "kernel": "k_bulk", "bytes_per_cell": bpc, "cells_per_launch": n_bulk,
+                         "launch_ms": res["bulk_ms"], "peak_source": f"{peak_kind} hbm_gbs"},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": res["launches_per_step"] * args.steps,
+            "variants": variants,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

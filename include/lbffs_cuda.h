@@ -1,0 +1,174 @@
+/*
+ * lbffs_cuda.h -- C ABI of the GB300 lattice-Boltzmann step for LBFFS.
+ *
+ * This header is the drop-in boundary for the OpenCL section of LBFFS's driver
+ * (D3Q19_opencl/ns.cpp:382-603, D3Q27_opencl/ns.cpp): one context replaces the
+ * cl::Context / cl::CommandQueue / 27 cl::Buffer objects / 4 KernelFunctors, and
+ * the host keeps computing everything else (input.hpp, setBoundaryConditions.hpp,
+ * walls.hpp, stl.hpp, initialization.hpp, restart.hpp, write.hpp) unchanged.
+ *
+ * Conventions
+ *  - Every call returns an int status: LBFFS_OK (0) or a negative LBFFS_E_* code.
+ *    lbffs_last_error() returns a message for the last failing call on a context
+ *    (or on the calling thread when the context pointer is NULL).  No C++
+ *    exception crosses the boundary.
+ *  - Arrays use the reference's layout: cell index ic = nx*ny*k + nx*j + i
+ *    (src/base.hpp:20), populations f[q*E + ic] with E = nx*ny*nz
+ *    (src/base.hpp:30), the reference's velocity order (D3Q19.hpp:14-27).
+ *  - Host pointers are borrowed for the duration of a call only.
+ *  - A context owns one CUDA stream and all of its device memory.  Calls on one
+ *    context must not overlap; separate contexts are independent.
+ *  - Nothing here allocates on the host side the caller must free.
+ */
+#ifndef LBFFS_CUDA_H
+#define LBFFS_CUDA_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBFFS_OK 0
+#define LBFFS_E_ARG (-1)     /* invalid argument (size, field id, enum value) */
+#define LBFFS_E_CUDA (-2)    /* a CUDA runtime call failed; see lbffs_last_error */
+#define LBFFS_E_STATE (-3)   /* call not valid in the current state */
+#define LBFFS_E_UNSUPPORTED (-4) /* feature present in the reference but not built (WallFunction code 7) */
+#define LBFFS_E_NONFINITE (-5)   /* a non-finite density was produced (divergence sentinel) */
+
+typedef struct lbffs_ctx lbffs_ctx;
+
+/* population storage in HBM; collision arithmetic is FP32 in every case */
+enum lbffs_storage {
+    LBFFS_FP32 = 0,  /* float, bit-compatible with the reference's buffers */
+    LBFFS_FP16S = 1, /* IEEE half of (f_q - w_q) * 2^15 */
+    LBFFS_BF16S = 2  /* bfloat16 of (f_q - w_q) */
+};
+enum lbffs_collision {
+    LBFFS_COLL_RR = 0,      /* recursive regularised (D3Q19 kernel.cl:3156; D3Q27: full Hermite basis) */
+    LBFFS_COLL_CUMULANT = 1 /* Geier cumulant (D3Q27 kernel.cl:2352), D3Q27 only */
+};
+enum lbffs_sgs {
+    LBFFS_SGS_SMAGORINSKY = 0, /* smagorinskyTauSGS with near-wall damping (kernel.cl:2133), honours LES */
+    LBFFS_SGS_WALE = 1         /* waleTauSGS (kernel.cl:2267), the reference's live model; ignores LES */
+};
+enum lbffs_wall {
+    LBFFS_WALL_BB = 0, /* half-way bounce-back on STL links (D3Q19 kernel.cl:1947) */
+    LBFFS_WALL_IBB = 1 /* Filippova-Hanel / Mei-Luo-Shyy interpolated bounce-back (D3Q27 kernel.cl:1847-1888) */
+};
+
+/* Lattice description; replaces the compile-time choice of D3Q19_opencl vs D3Q27_opencl. */
+typedef struct lbffs_desc {
+    int nx, ny, nz;  /* input.txt nx ny nz */
+    int q;           /* 19 or 27 */
+    int storage;     /* enum lbffs_storage */
+    int collision;   /* enum lbffs_collision */
+    int sgs;         /* enum lbffs_sgs */
+    int wall;        /* enum lbffs_wall */
+    int device;      /* CUDA device ordinal */
+    float cs;        /* Smagorinsky constant (the reference's live value is 0.1, kernel.cl:3628) */
+} lbffs_desc;
+
+/* Field ids: the reference's device buffers (ns.cpp:405-436). */
+enum lbffs_field {
+    LBFFS_F = 0,         /* float32[Q*E] populations (f_d); converted to/from the storage format */
+    LBFFS_BOUNDARY = 1,  /* int32[E] 1 on domain-face cells (boundary_d) */
+    LBFFS_BOUNDARY1 = 2, /* int32[E] x-face BC code (boundary1_d), src/input.hpp:221-256 */
+    LBFFS_BOUNDARY2 = 3, /* int32[E] y-face BC code */
+    LBFFS_BOUNDARY3 = 4, /* int32[E] z-face BC code */
+    LBFFS_SDF = 5,       /* float32[E] wall distance, 10000 = none (sdf_d) */
+    LBFFS_SOLID = 6,     /* uint8[E] (solid_d) */
+    LBFFS_NEISOLID = 7,  /* uint8[E] (neiSolid_d) */
+    LBFFS_U0 = 8,        /* float32[E] wall / inlet velocity (u0_d) */
+    LBFFS_V0 = 9,
+    LBFFS_W0 = 10,
+    LBFFS_OMEGA = 11,    /* float32[E] relaxation rate (omega_d) */
+    LBFFS_TAUSGS = 12,   /* float32[E] eddy relaxation time (tauSGS_d) */
+    LBFFS_RHO = 13,      /* float32[E] (rho_d) */
+    LBFFS_U = 14,        /* float32[E] (u_d) */
+    LBFFS_V = 15,
+    LBFFS_W = 16,
+    LBFFS_FWX = 17,      /* float32[E] STL-link wall force (Fwx_d) */
+    LBFFS_FWY = 18,
+    LBFFS_FWZ = 19,
+    LBFFS_GXIBM = 20,    /* float32[E] IBM forcing field (GxIBM_d) */
+    LBFFS_GYIBM = 21,
+    LBFFS_GZIBM = 22,
+    LBFFS_NFIELDS = 23
+};
+
+/* Per-step scalars: the trailing arguments of k_streamingCollision (ns.cpp:528-535). */
+typedef struct lbffs_step_params {
+    float dpdx;       /* lattice-unit pressure gradient (x) */
+    float rho_av;     /* carried for interface parity; unused by the step, as in the reference */
+    float les;        /* LES switch as float 0/1 */
+    float omega_b;    /* bulk relaxation rate (omegaB, default 0.1) */
+    float spz_width;  /* sponge width as a fraction of the domain (spzWidth, default 0.1) */
+    float clim;       /* cumulant limiter (clim, default 0.01), D3Q27 */
+    int store_fields; /* 0: macroscopic fields only where the step itself needs them;
+                         1: rho/u/v/w/tauSGS of every fluid cell on the last step of the call;
+                         2: on every step (what the reference does) */
+} lbffs_step_params;
+
+/* Create a context (replaces ns.cpp:385-436 context/queue/buffer creation).
+   Device memory is zero-initialised except SDF = 10000 and OMEGA = 1. */
+int lbffs_create(const lbffs_desc* desc, lbffs_ctx** out);
+/* Release a context and all its device memory. */
+int lbffs_destroy(lbffs_ctx* ctx);
+/* Message of the last error on ctx (or on this thread if ctx is NULL). Never NULL. */
+const char* lbffs_last_error(const lbffs_ctx* ctx);
+
+/* Host -> device copy of one field (the cl::Buffer(context, begin, end, true) copies of
+   ns.cpp:405-436).  bytes must equal the field size.  Geometry fields take effect at the
+   next lbffs_step. */
+int lbffs_upload(lbffs_ctx* ctx, int field, const void* host, size_t bytes);
+/* Device -> host copy (cl::copy(queue, X_d, X.begin(), X.end()) of write.hpp:3-14). */
+int lbffs_download(lbffs_ctx* ctx, int field, void* host, size_t bytes);
+
+/* Advance nsteps time steps: each is one k_streamingCollision launch (ns.cpp:514-536), the
+   IBM sub-step when markers are set (ns.cpp:542-601), and the f/fTmp swap (ns.cpp:602).
+   Asynchronous on the context stream; errors of earlier launches are reported. */
+int lbffs_step(lbffs_ctx* ctx, const lbffs_step_params* params, int nsteps);
+/* Wait for the context stream (queue.finish()); reports the divergence sentinel. */
+int lbffs_synchronize(lbffs_ctx* ctx);
+
+/* FP64 sum of the STL-link wall force over fluid cells: SumFwx/y/z of write.hpp:25-46,
+   accumulated in double instead of float. */
+int lbffs_force_sum(lbffs_ctx* ctx, double out[3]);
+/* FP64 sum of rho over fluid cells computed from the populations (write.hpp:25-46). */
+int lbffs_mass(lbffs_ctx* ctx, double* out);
+
+/* STL link table (bit q of mask set: population q of cell is a link, neiSolid && solid
+   upwind, kernel.cl:1940-1943).  Writes min(n, capacity) entries in ascending cell order
+   and the total count to *n.  Pass capacity 0 to query the count. */
+int lbffs_links(lbffs_ctx* ctx, long long* cells, unsigned* masks, long long capacity, long long* n);
+
+/* IBM markers (movingSTLcList, ns.cpp:248-254): n markers, xyz in lattice units. */
+int lbffs_set_markers(lbffs_ctx* ctx, const float* xyz, int n);
+int lbffs_get_markers(lbffs_ctx* ctx, float* xyz, int n);
+/* Marker motion (readMotions, walls.hpp:586-629) plus an optional sinusoidal displacement
+   amp*sin(2*pi*t/period) (period <= 0: none); t counts steps from set_motion. */
+typedef struct lbffs_motion {
+    float u_trans, v_trans, w_trans;    /* per-step translation */
+    float rot_x, rot_y, rot_z;          /* rotation centre */
+    float axis_x, axis_y, axis_z;       /* rotation axis (unit) */
+    float rot_omega;                    /* rotation angle per step */
+    float amp_x, amp_y, amp_z, period;  /* sinusoidal displacement */
+} lbffs_motion;
+int lbffs_set_motion(lbffs_ctx* ctx, const lbffs_motion* motion);
+/* FP64 sum of the IBM forcing over fluid cells (SumGxIBM.. of write.hpp:25-46). */
+int lbffs_ibm_force_sum(lbffs_ctx* ctx, double out[3]);
+
+/* The context's cudaStream_t (for callers that order their own work after the step). */
+int lbffs_get_stream(lbffs_ctx* ctx, void** stream);
+/* Per-kernel device time (CUDA events around each launch) once enabled.  name is "bulk",
+   "special" or "ibm"; returns accumulated milliseconds and launch count. */
+int lbffs_set_timing(lbffs_ctx* ctx, int enabled);
+int lbffs_kernel_time(lbffs_ctx* ctx, const char* name, double* total_ms, long long* launches);
+/* Counts of cells per class after the geometry commit: [fluid, special, link, store]. */
+int lbffs_cell_counts(lbffs_ctx* ctx, long long out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

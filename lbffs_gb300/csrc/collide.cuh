@@ -1,0 +1,324 @@
+// Device collision operators of the fused step.  All loops run over compile-time
+// bounds and are fully unrolled, so the populations and moments live in registers.
+//
+//  collide_rr<19>   recursive-regularised collision of D3Q19_opencl/kernel.cl:3156-3309:
+//                   second-order Hermite moments, bulk/shear split of the diagonal
+//                   (omega_P / omega_M from omega_B), recursive third (c_a^2 c_b) and
+//                   fourth (c_a^2 c_b^2) order non-equilibrium terms, D3Q19 raw-moment
+//                   inverse, first-order pressure-gradient source rho w_q 3 c_qx dpdx.
+//  collide_rr<27>   the same closure on the full D3Q27 tensor Hermite basis (no reference
+//                   counterpart; defined with the CPU oracle): every coefficient of order
+//                   >= 3 is u-products + (1 - omega) * its recursive non-equilibrium part.
+//  collide_cumulant the parametrised cumulant operator (Geier et al. 2015) as run by
+//                   D3Q27_opencl/kernel.cl:2352-2691, including its clim limiter and its
+//                   fifth-order back-conversion products.
+#pragma once
+#include "lbffs_common.cuh"
+
+namespace lbffs {
+
+// c_a^{n} for n in 0..2 with c in {-1,0,1}, evaluated at compile time after unrolling
+__device__ __forceinline__ float ipow(float x, int n) { return n == 0 ? 1.f : n == 1 ? x : x * x; }
+
+template <int Q>
+__device__ __forceinline__ void rr_second_order(const float (&ft)[Q], float rho, const float (&U)[3], float we,
+                                                float omega_b, float (&N2)[3][3], float (&R2)[3][3])
+{
+    float M2[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) M2[a][b] = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = a; b < 3; b++) {
+                const int cc = lat_c(Q, q, a) * lat_c(Q, q, b);
+                if (a == b) M2[a][b] += ((float)cc - 1.f / 3.f) * ft[q];
+                else if (cc != 0) M2[a][b] += (float)cc * ft[q];
+            }
+    }
+    const float ir = 1.f / rho;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = a; b < 3; b++) {
+            M2[a][b] *= ir;
+            N2[a][b] = M2[a][b] - U[a] * U[b];
+            N2[b][a] = N2[a][b];
+        }
+    const float wm = (omega_b - we) * (1.f / 3.f), wp = wm + we;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float r = M2[a][a];
+#pragma unroll
+        for (int b = 0; b < 3; b++) r -= (a == b ? wp : wm) * N2[b][b];
+        R2[a][a] = r;
+#pragma unroll
+        for (int b = a + 1; b < 3; b++) {
+            R2[a][b] = M2[a][b] - we * N2[a][b];
+            R2[b][a] = R2[a][b];
+        }
+    }
+}
+
+// D3Q19 recursive regularised collision; U is the velocity with the half-force shift removed.
+__device__ __forceinline__ void collide_rr19(float (&f)[19], float rho, const float (&U)[3], float we, float omega_b,
+                                             float dpdx)
+{
+    float N2[3][3], R2[3][3];
+    rr_second_order<19>(f, rho, U, we, omega_b, N2, R2);
+    const float third = 1.f / 3.f, ninth = 1.f / 9.f, k1 = 1.f - we;
+    float T3[3][3], Q4[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            if (a == b) continue;
+            const float n3 = U[b] * N2[a][a] + 2.f * U[a] * N2[a][b];
+            T3[a][b] = U[a] * U[a] * U[b] + k1 * n3 + third * U[b];
+            const float n4 = U[b] * U[b] * N2[a][a] + U[a] * U[a] * N2[b][b] + 4.f * U[a] * U[b] * N2[a][b];
+            Q4[a][b] = U[a] * U[a] * U[b] * U[b] + k1 * n4 + third * (R2[a][a] + R2[b][b]) + ninth;
+        }
+    const float RM[3] = {R2[0][0] + third, R2[1][1] + third, R2[2][2] + third};
+    const float src = rho * 3.f * dpdx;
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        const int cx = lat_c(19, q, 0), cy = lat_c(19, q, 1), cz = lat_c(19, q, 2);
+        const int n2 = lat_n2(19, q);
+        float val;
+        if (n2 == 0) {
+            val = rho * (1.f - RM[0] - RM[1] - RM[2] + Q4[0][1] + Q4[0][2] + Q4[1][2]);
+        } else if (n2 == 1) {
+            const int a = cx ? 0 : cy ? 1 : 2, b = (a + 1) % 3, d = (a + 2) % 3;
+            const float s = (float)(a == 0 ? cx : a == 1 ? cy : cz);
+            val = 0.5f * rho * (s * U[a] + RM[a] - s * T3[b][a] - s * T3[d][a] - Q4[a][b] - Q4[a][d]);
+        } else {
+            const int a = cx ? 0 : 1, b = cz ? 2 : 1;
+            const float sa = (float)(a == 0 ? cx : cy), sb = (float)(b == 2 ? cz : cy);
+            val = 0.25f * rho * (sa * sb * R2[a][b] + sb * T3[a][b] + sa * T3[b][a] + Q4[a][b]);
+        }
+        if (cx != 0) val += lat_w(19, q) * (float)cx * src;
+        f[q] = val;
+    }
+}
+
+// 1-D backward chimera step (central moments about u -> populations at c = -1, 0, +1)
+__device__ __forceinline__ void chimera_back(float k0, float k1, float k2, float u, float& fm, float& f0, float& fp)
+{
+    f0 = k0 * (1.f - u * u) - 2.f * u * k1 - k2;
+    fm = 0.5f * (k0 * (u * u - u) + k1 * (2.f * u - 1.f) + k2);
+    fp = 0.5f * (k0 * (u * u + u) + k1 * (2.f * u + 1.f) + k2);
+}
+
+__device__ __forceinline__ void moments_to_pop27(float (&M)[3][3][3], float u, float v, float w, float (&f)[27])
+{
+    float P[3][3][3];
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) chimera_back(M[0][b][c], M[1][b][c], M[2][b][c], u, P[0][b][c], P[1][b][c], P[2][b][c]);
+#pragma unroll
+    for (int s = 0; s < 3; s++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) chimera_back(P[s][0][c], P[s][1][c], P[s][2][c], v, M[s][0][c], M[s][1][c], M[s][2][c]);
+#pragma unroll
+    for (int s = 0; s < 3; s++)
+#pragma unroll
+        for (int t = 0; t < 3; t++) chimera_back(M[s][t][0], M[s][t][1], M[s][t][2], w, P[s][t][0], P[s][t][1], P[s][t][2]);
+#pragma unroll
+    for (int q = 0; q < 27; q++) f[q] = P[lat_c(27, q, 0) + 1][lat_c(27, q, 1) + 1][lat_c(27, q, 2) + 1];
+}
+
+// D3Q27 recursive regularised collision on the tensor Hermite basis; U without the half-force shift.
+__device__ __forceinline__ void collide_rr27(float (&f)[27], float rho, const float (&U)[3], float we, float omega_b,
+                                             float dpdx)
+{
+    float N2[3][3], R2[3][3];
+    rr_second_order<27>(f, rho, U, we, omega_b, N2, R2);
+    const float third = 1.f / 3.f, k1 = 1.f - we;
+    float H[3][3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int n = a + b + c;
+                if (n == 0) {
+                    H[a][b][c] = 1.f;
+                } else if (n == 1) {
+                    H[a][b][c] = a ? U[0] : b ? U[1] : U[2];
+                } else if (n == 2) {
+                    const int p = a ? 0 : 1, r = c ? 2 : (b ? 1 : 0);
+                    const int pp = (a == 2) ? 0 : (b == 2) ? 1 : (c == 2) ? 2 : p;
+                    const int rr = (a == 2) ? 0 : (b == 2) ? 1 : (c == 2) ? 2 : r;
+                    H[a][b][c] = R2[pp][rr];
+                } else {
+                    const float eq = ipow(U[0], a) * ipow(U[1], b) * ipow(U[2], c);
+                    float neq = 0.f;
+                    if (a == 2) neq += N2[0][0] * ipow(U[1], b) * ipow(U[2], c);
+                    if (b == 2) neq += N2[1][1] * ipow(U[0], a) * ipow(U[2], c);
+                    if (c == 2) neq += N2[2][2] * ipow(U[0], a) * ipow(U[1], b);
+                    if (a && b) neq += (float)(a * b) * N2[0][1] * ipow(U[0], a - 1) * ipow(U[1], b - 1) * ipow(U[2], c);
+                    if (a && c) neq += (float)(a * c) * N2[0][2] * ipow(U[0], a - 1) * ipow(U[1], b) * ipow(U[2], c - 1);
+                    if (b && c) neq += (float)(b * c) * N2[1][2] * ipow(U[0], a) * ipow(U[1], b - 1) * ipow(U[2], c - 1);
+                    H[a][b][c] = eq + k1 * neq;
+                }
+            }
+    float M[3][3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                float s = 0.f;
+#pragma unroll
+                for (int ta = 0; ta < 2; ta++)
+#pragma unroll
+                    for (int tb = 0; tb < 2; tb++)
+#pragma unroll
+                        for (int tc = 0; tc < 2; tc++) {
+                            if ((ta && a != 2) || (tb && b != 2) || (tc && c != 2)) continue;
+                            const float coef = (ta ? third : 1.f) * (tb ? third : 1.f) * (tc ? third : 1.f);
+                            s += coef * H[ta ? 0 : a][tb ? 0 : b][tc ? 0 : c];
+                        }
+                M[a][b][c] = rho * s;
+            }
+    moments_to_pop27(M, 0.f, 0.f, 0.f, f);
+    const float src = rho * 3.f * dpdx;
+#pragma unroll
+    for (int q = 0; q < 27; q++)
+        if (lat_c(27, q, 0) != 0) f[q] += lat_w(27, q) * (float)lat_c(27, q, 0) * src;
+}
+
+// Cumulant collision (D3Q27_opencl/kernel.cl:2352-2691); u is the velocity including the half-force shift.
+__device__ __forceinline__ void collide_cumulant(float (&f)[27], float rho, float u, float v, float w, float we,
+                                                 float omega_b, float clim)
+{
+    float K[3][3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) K[a][b][c] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+        const float dx = (float)lat_c(27, q, 0) - u, dy = (float)lat_c(27, q, 1) - v, dz = (float)lat_c(27, q, 2) - w;
+        const float px[3] = {1.f, dx, dx * dx}, py[3] = {1.f, dy, dy * dy}, pz[3] = {1.f, dz, dz * dz};
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    if (a + b + c > 0) K[a][b][c] += px[a] * py[b] * pz[c] * f[q];
+    }
+    K[0][0][0] = rho;
+    const float ir = 1.f / rho;
+    const float C200 = K[2][0][0], C020 = K[0][2][0], C002 = K[0][0][2];
+    const float C110 = K[1][1][0], C101 = K[1][0][1], C011 = K[0][1][1];
+    const float C210 = K[2][1][0], C201 = K[2][0][1], C021 = K[0][2][1], C120 = K[1][2][0], C102 = K[1][0][2],
+                C012 = K[0][1][2], C111 = K[1][1][1];
+    const float C211 = K[2][1][1] - (K[2][0][0] * K[0][1][1] + 2.f * K[1][1][0] * K[1][0][1]) * ir;
+    const float C121 = K[1][2][1] - (K[0][2][0] * K[1][0][1] + 2.f * K[1][1][0] * K[0][1][1]) * ir;
+    const float C112 = K[1][1][2] - (K[0][0][2] * K[1][1][0] + 2.f * K[1][0][1] * K[0][1][1]) * ir;
+    const float C220 = K[2][2][0] - (K[2][0][0] * K[0][2][0] + 2.f * K[1][1][0] * K[1][1][0]) * ir;
+    const float C202 = K[2][0][2] - (K[0][0][2] * K[2][0][0] + 2.f * K[1][0][1] * K[1][0][1]) * ir;
+    const float C022 = K[0][2][2] - (K[0][2][0] * K[0][0][2] + 2.f * K[0][1][1] * K[0][1][1]) * ir;
+    const float C122 = K[1][2][2] - (K[0][0][2] * K[1][2][0] + K[0][2][0] * K[1][0][2] + 4.f * K[0][1][1] * K[1][1][1] +
+                                     2.f * (K[1][0][1] * K[0][2][1] + K[1][1][0] * K[0][1][2])) * ir;
+    const float C212 = K[2][1][2] - (K[2][0][0] * K[0][1][2] + K[0][0][2] * K[2][1][0] + 4.f * K[1][0][1] * K[1][1][1] +
+                                     2.f * (K[1][1][0] * K[1][0][2] + K[0][1][1] * K[2][0][1])) * ir;
+    const float C221 = K[2][2][1] - (K[0][2][0] * K[2][0][1] + K[2][0][0] * K[0][2][1] + 4.f * K[1][1][0] * K[1][1][1] +
+                                     2.f * (K[0][1][1] * K[2][1][0] + K[1][0][1] * K[1][2][0])) * ir;
+    // C222 relaxes to 0 (omega10 = 1, kernel.cl:2478), so it is not formed.
+
+    const float w1 = we, w2 = omega_b;
+    const float w3 = 8.f * (w1 - 2.f) * (w2 * (3.f * w1 - 1.f) - 5.f * w1) /
+                     (8.f * (5.f - 2.f * w1) * w1 + w2 * (8.f + w1 * (9.f * w1 - 26.f)));
+    const float w4 = 8.f * (w1 - 2.f) * (w1 + w2 * (3.f * w1 - 7.f)) / (w2 * (56.f - 42.f * w1 + 9.f * w1 * w1) - 8.f * w1);
+    const float w5 = 24.f * (w1 - 2.f) * (4.f * w1 * w1 + w1 * w2 * (18.f - 13.f * w1) + w2 * w2 * (2.f + w1 * (6.f * w1 - 11.f))) /
+                     (16.f * w1 * w1 * (w1 - 6.f) - 2.f * w1 * w2 * (216.f + 5.f * w1 * (9.f * w1 - 46.f)) +
+                      w2 * w2 * (w1 * (3.f * w1 - 10.f) * (15.f * w1 - 28.f) - 48.f));
+    auto lim = [&](float wr, float x) {
+        const float ax = fabsf(x);
+        return ax > 0.f ? wr + (1.f - wr) * ax / (ax + clim * rho) : 1.f;
+    };
+    const float w3a = lim(w3, C120 + C102), w3b = lim(w3, C210 + C012), w3c = lim(w3, C201 + C021);
+    const float w4a = lim(w4, C120 - C102), w4b = lim(w4, C210 - C012), w4c = lim(w4, C201 - C021);
+    const float w5l = lim(w5, C111);
+    float A = (4.f * w1 * w1 + 2.f * w1 * w2 * (w1 - 6.f) + w2 * w2 * (w1 * (10.f - 3.f * w1) - 4.f)) /
+              ((w1 - w2) * (w2 * (2.f + 3.f * w1) - 8.f * w1));
+    float B = (4.f * w1 * w2 * (9.f * w1 - 16.f) - 4.f * w1 * w1 - 2.f * w2 * w2 * (2.f + 9.f * w1 * (w1 - 2.f))) /
+              (3.f * (w1 - w2) * (w2 * (2.f + 3.f * w1) - 8.f * w1));
+    A = fmaxf(A, 0.f);
+    B = fmaxf(B, 0.f);
+
+    const float K000 = rho;
+    const float Dxu = -0.5f * (w1 * (2.f * C200 - C020 - C002) + w2 * (C200 + C020 + C002 - K000)) * ir;
+    const float Dyv = Dxu + 1.5f * w1 * (C200 - C020) * ir;
+    const float Dzw = Dxu + 1.5f * w1 * (C200 - C002) * ir;
+    const float Dxv = -3.f * w1 * C110 * ir, Dxw = -3.f * w1 * C101 * ir, Dyw = -3.f * w1 * C011 * ir;
+    float X1 = (1.f - w1) * (C200 - C020) - 3.f * rho * (1.f - 0.5f * w1) * (u * u * Dxu - v * v * Dyv);
+    float X2 = (1.f - w1) * (C200 - C002) - 3.f * rho * (1.f - 0.5f * w1) * (u * u * Dxu - w * w * Dzw);
+    float X3 = K000 * w2 + (1.f - w2) * (C200 + C020 + C002) - 3.f * rho * (1.f - 0.5f * w2) * (u * u * Dxu + v * v * Dyv + w * w * Dzw);
+    float M[3][3][3];
+    M[0][0][0] = K000;
+    M[1][0][0] = -K[1][0][0];
+    M[0][1][0] = -K[0][1][0];
+    M[0][0][1] = -K[0][0][1];
+    M[2][0][0] = (X1 + X2 + X3) * (1.f / 3.f);
+    M[0][2][0] = M[2][0][0] - X1;
+    M[0][0][2] = M[2][0][0] - X2;
+    M[1][1][0] = (1.f - w1) * C110;
+    M[1][0][1] = (1.f - w1) * C101;
+    M[0][1][1] = (1.f - w1) * C011;
+    X1 = (1.f - w3a) * (C120 + C102);
+    X2 = (1.f - w4a) * (C120 - C102);
+    M[1][2][0] = 0.5f * (X1 + X2);
+    M[1][0][2] = 0.5f * (X1 - X2);
+    X1 = (1.f - w3b) * (C210 + C012);
+    X2 = (1.f - w4b) * (C210 - C012);
+    M[2][1][0] = 0.5f * (X1 + X2);
+    M[0][1][2] = 0.5f * (X1 - X2);
+    X1 = (1.f - w3c) * (C201 + C021);
+    X2 = (1.f - w4c) * (C201 - C021);
+    M[2][0][1] = 0.5f * (X1 + X2);
+    M[0][2][1] = 0.5f * (X1 - X2);
+    M[1][1][1] = (1.f - w5l) * C111;
+    const float tw = 1.f / w1 - 0.5f;
+    // omega6..omega10 = 1 (kernel.cl:2474-2478): the fourth- to sixth-order cumulants relax to equilibrium
+    X1 = 2.f * tw * A * rho * (Dxu - 2.f * Dyv + Dzw) * (1.f / 3.f);
+    X2 = 2.f * tw * A * rho * (Dxu + Dyv - 2.f * Dzw) * (1.f / 3.f);
+    X3 = -4.f * tw * A * rho * (Dxu + Dyv + Dzw) * (1.f / 3.f);
+    const float Cs220 = (X1 + X2 + X3) * (1.f / 3.f), Cs202 = -(X1 - X3) * (1.f / 3.f), Cs022 = -(X2 - X3) * (1.f / 3.f);
+    const float Cs211 = -tw * B * rho * Dyw * (1.f / 3.f);
+    const float Cs121 = -tw * B * rho * Dxw * (1.f / 3.f);
+    const float Cs112 = -tw * B * rho * Dxv * (1.f / 3.f);
+    M[2][1][1] = Cs211 + (M[2][0][0] * M[0][1][1] + 2.f * M[1][1][0] * M[1][0][1]) * ir;
+    M[1][2][1] = Cs121 + (M[0][2][0] * M[1][0][1] + 2.f * M[0][1][1] * M[1][1][0]) * ir;
+    M[1][1][2] = Cs112 + (M[0][0][2] * M[1][1][0] + 2.f * M[1][0][1] * M[0][1][1]) * ir;
+    M[2][2][0] = Cs220 + (M[2][0][0] * M[0][2][0] + 2.f * M[1][1][0] * M[1][1][0]) * ir;
+    M[2][0][2] = Cs202 + (M[0][0][2] * M[2][0][0] + 2.f * M[1][0][1] * M[1][0][1]) * ir;
+    M[0][2][2] = Cs022 + (M[0][2][0] * M[0][0][2] + 2.f * M[0][1][1] * M[0][1][1]) * ir;
+    M[1][2][2] = (M[0][2][2] * M[1][2][0] + M[0][2][0] * M[1][0][2] + 4.f * M[0][1][1] * M[1][1][1] +
+                  2.f * (M[1][0][1] * M[0][2][1] + M[1][1][0] * M[0][1][2])) * ir;
+    M[2][1][2] = (M[2][0][2] * M[0][1][2] + M[0][0][2] * M[2][1][0] + 4.f * M[1][0][1] * M[1][1][1] +
+                  2.f * (M[1][1][0] * M[1][0][2] + M[0][1][1] * M[2][0][1])) * ir;
+    M[2][2][1] = (M[2][2][0] * M[2][0][1] + M[2][0][0] * M[0][2][1] + 4.f * M[1][1][0] * M[1][1][1] +
+                  2.f * (M[0][1][1] * M[2][1][0] + M[1][0][1] * M[1][2][0])) * ir;
+    M[2][2][2] = (4.f * M[1][1][1] * M[1][1][1] + M[2][0][0] * M[0][2][2] + M[0][2][0] * M[2][0][2] + M[0][0][2] * M[2][2][0] +
+                  4.f * (M[0][1][1] * M[2][1][1] + M[1][0][1] * M[1][2][1] + M[1][1][0] * M[1][1][2]) +
+                  2.f * (M[1][2][0] * M[1][0][2] + M[2][1][0] * M[0][1][2] + M[2][0][1] * M[0][2][1])) * ir -
+                 (16.f * M[1][1][0] * M[1][0][1] * M[0][1][1] +
+                  4.f * (M[1][0][1] * M[1][0][1] * M[0][2][0] + M[0][1][1] * M[0][1][1] * M[2][0][0] + M[1][1][0] * M[1][1][0] * M[0][0][2]) +
+                  2.f * M[2][0][0] * M[0][2][0] * M[0][0][2]) * ir * ir;
+    moments_to_pop27(M, u, v, w, f);
+}
+
+}  // namespace lbffs

@@ -1,0 +1,44 @@
+// Host-side launcher declarations shared by the C-ABI layer and the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lbffs_common.cuh"
+
+namespace lbffs {
+
+struct StepConfig {
+    int storage, collision, sgs, wall;
+    bool les;  // Smagorinsky with a non-zero LES switch
+};
+
+// One half of a time step: bulk=true launches k_bulk, bulk=false launches k_special.
+cudaError_t launch_q19(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st);
+cudaError_t launch_q27(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st);
+
+// setup.cu
+cudaError_t setup_pack_bc(const int* boundary, const int* b1, const int* b2, const int* b3, uint16_t* bc, int nx,
+                          int ny, int nz, cudaStream_t st);
+cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
+                           const float* omega, float omega0, float cs, uint8_t* flags, uint8_t* scratch, int nx, int ny,
+                           int nz, cudaStream_t st);
+// counts[nblocks] of FL_SPECIAL cells per chunk of SETUP_CHUNK cells
+constexpr int SETUP_CHUNK = 256;
+cudaError_t setup_count_special(const uint8_t* flags, long long E, unsigned* counts, cudaStream_t st);
+cudaError_t setup_scatter_special(const uint8_t* flags, long long E, const unsigned long long* offsets,
+                                  uint32_t* out, cudaStream_t st);
+cudaError_t setup_link_masks(int Q, const uint32_t* special, long long n, const uint16_t* bc, const uint8_t* solid,
+                             const uint8_t* nei, int nx, int ny, int nz, uint32_t* masks, cudaStream_t st);
+cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long start, long long count, long long E,
+                     cudaStream_t st);
+cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long start, long long count, long long E,
+                     cudaStream_t st);
+cudaError_t fill_f32(float* p, float v, long long n, cudaStream_t st);
+// FP64 partial sums: force over the listed cells (3 per block), mass over fluid cells (1 per block)
+constexpr int REDUCE_BS = 256;
+cudaError_t reduce_force(const uint32_t* cells, long long n, const float* fx, const float* fy, const float* fz,
+                         double* partial, int nblocks, cudaStream_t st);
+cudaError_t reduce_mass(int storage, int Q, const void* f, const uint8_t* flags, long long E, double* partial,
+                        int nblocks, cudaStream_t st);
+
+}  // namespace lbffs

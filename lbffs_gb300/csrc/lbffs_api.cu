@@ -1,0 +1,772 @@
+// C-ABI implementation (include/lbffs_cuda.h): context lifetime, field transfer,
+// geometry commit, the step loop and reductions.  Host code only; kernels live in
+// step_d3q19.cu, step_d3q27.cu, setup.cu and ibm.cu.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbffs_cuda.h"
+#include "ibm.h"
+#include "launch.h"
+
+using namespace lbffs;
+
+namespace {
+
+thread_local std::string g_thread_error = "no error";
+
+enum FieldKind { K_F, K_INT, K_U8, K_FLOAT, K_MACRO };
+
+struct FieldInfo {
+    FieldKind kind;
+    int macro;  // index into the macro buffers for K_MACRO
+};
+
+FieldInfo field_info(int f)
+{
+    switch (f) {
+        case LBFFS_F: return {K_F, -1};
+        case LBFFS_BOUNDARY:
+        case LBFFS_BOUNDARY1:
+        case LBFFS_BOUNDARY2:
+        case LBFFS_BOUNDARY3: return {K_INT, -1};
+        case LBFFS_SOLID:
+        case LBFFS_NEISOLID: return {K_U8, -1};
+        case LBFFS_RHO: return {K_MACRO, 0};
+        case LBFFS_U: return {K_MACRO, 1};
+        case LBFFS_V: return {K_MACRO, 2};
+        case LBFFS_W: return {K_MACRO, 3};
+        case LBFFS_TAUSGS: return {K_MACRO, 4};
+        default: return {K_FLOAT, -1};
+    }
+}
+
+}  // namespace
+
+struct lbffs_ctx {
+    lbffs_desc d{};
+    int Q = 19;
+    long long E = 0;
+    size_t tsize = 4;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    std::string err = "no error";
+
+    void* f[2] = {nullptr, nullptr};
+    int fcur = 0;
+    int* iarr[4] = {nullptr, nullptr, nullptr, nullptr};  // boundary, boundary1..3 as uploaded
+    uint8_t *solid = nullptr, *nei = nullptr, *flags = nullptr;
+    uint16_t* bc = nullptr;
+    float *u0 = nullptr, *v0 = nullptr, *w0 = nullptr, *omega = nullptr, *sdf = nullptr;
+    float* macro[2][5] = {{nullptr}};
+    int mcur = 0;
+    float* fw[3] = {nullptr, nullptr, nullptr};
+    float* g[3] = {nullptr, nullptr, nullptr};
+    uint32_t* special = nullptr;
+    long long n_special = 0;
+    long long counts[4] = {0, 0, 0, 0};
+    float omega0 = 1.f;
+    int sponge_mask = 0;
+    bool dirty = true;
+    int* d_err = nullptr;
+    float* stage = nullptr;
+    size_t stage_elems = 0;
+    double* partial = nullptr;
+    int partial_blocks = 0;
+
+    // IBM
+    int n_markers = 0;
+    float* markers = nullptr;
+    float* gm = nullptr;
+    double* ibm_acc = nullptr;
+    double* ibm_lag = nullptr;
+    int* ibm_box = nullptr;
+    long long* ibm_t = nullptr;
+    IbmMotion motion{};
+
+    // timing
+    bool timing = false;
+    struct Ev {
+        cudaEvent_t a, b;
+        int kind;
+    };
+    std::vector<Ev> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[3] = {0, 0, 0};
+    long long launches[3] = {0, 0, 0};
+};
+
+static int fail(lbffs_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    g_thread_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail(c, LBFFS_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+    } while (0)
+
+template <class T>
+static cudaError_t dalloc(T** p, size_t n)
+{
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T) + 16);
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, n * sizeof(T) + 16);
+    return e;
+}
+
+static size_t field_bytes(const lbffs_ctx* c, int f)
+{
+    FieldInfo fi = field_info(f);
+    switch (fi.kind) {
+        case K_F: return sizeof(float) * (size_t)c->Q * (size_t)c->E;
+        case K_U8: return (size_t)c->E;
+        default: return 4 * (size_t)c->E;
+    }
+}
+
+static void* field_ptr(lbffs_ctx* c, int f)
+{
+    switch (f) {
+        case LBFFS_BOUNDARY: return c->iarr[0];
+        case LBFFS_BOUNDARY1: return c->iarr[1];
+        case LBFFS_BOUNDARY2: return c->iarr[2];
+        case LBFFS_BOUNDARY3: return c->iarr[3];
+        case LBFFS_SOLID: return c->solid;
+        case LBFFS_NEISOLID: return c->nei;
+        case LBFFS_SDF: return c->sdf;
+        case LBFFS_U0: return c->u0;
+        case LBFFS_V0: return c->v0;
+        case LBFFS_W0: return c->w0;
+        case LBFFS_OMEGA: return c->omega;
+        case LBFFS_FWX: return c->fw[0];
+        case LBFFS_FWY: return c->fw[1];
+        case LBFFS_FWZ: return c->fw[2];
+        case LBFFS_GXIBM: return c->g[0];
+        case LBFFS_GYIBM: return c->g[1];
+        case LBFFS_GZIBM: return c->g[2];
+        default: return nullptr;
+    }
+}
+
+static bool geometry_field(int f)
+{
+    return f == LBFFS_BOUNDARY || f == LBFFS_BOUNDARY1 || f == LBFFS_BOUNDARY2 || f == LBFFS_BOUNDARY3 ||
+           f == LBFFS_SOLID || f == LBFFS_NEISOLID || f == LBFFS_SDF || f == LBFFS_OMEGA;
+}
+
+extern "C" const char* lbffs_last_error(const lbffs_ctx* c) { return c ? c->err.c_str() : g_thread_error.c_str(); }
+
+extern "C" int lbffs_destroy(lbffs_ctx* c)
+{
+    if (!c) return LBFFS_OK;
+    cudaSetDevice(c->d.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    void* ptrs[] = {c->f[0], c->f[1], c->iarr[0], c->iarr[1], c->iarr[2], c->iarr[3], c->solid, c->nei, c->flags,
+                    c->bc, c->u0, c->v0, c->w0, c->omega, c->sdf, c->fw[0], c->fw[1], c->fw[2], c->g[0], c->g[1],
+                    c->g[2], c->special, c->d_err, c->stage, c->partial, c->markers, c->gm, c->ibm_acc, c->ibm_lag,
+                    c->ibm_box, c->ibm_t};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (auto& row : c->macro)
+        for (float* p : row)
+            if (p) cudaFree(p);
+    for (auto& e : c->pending) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    for (auto e : c->pool) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_create(const lbffs_desc* desc, lbffs_ctx** out)
+{
+    lbffs_ctx* c = nullptr;
+    if (!desc || !out) return fail(c, LBFFS_E_ARG, "lbffs_create: null argument");
+    *out = nullptr;
+    const lbffs_desc& d = *desc;
+    if (d.nx < 1 || d.ny < 1 || d.nz < 1 || d.ny > 65535 || d.nz > 65535)
+        return fail(c, LBFFS_E_ARG, "lbffs_create: grid extents must be >= 1 and ny, nz <= 65535");
+    if (d.q != 19 && d.q != 27) return fail(c, LBFFS_E_ARG, "lbffs_create: q must be 19 or 27");
+    if (d.storage < LBFFS_FP32 || d.storage > LBFFS_BF16S) return fail(c, LBFFS_E_ARG, "lbffs_create: bad storage");
+    if (d.collision != LBFFS_COLL_RR && d.collision != LBFFS_COLL_CUMULANT)
+        return fail(c, LBFFS_E_ARG, "lbffs_create: bad collision");
+    if (d.q == 19 && d.collision == LBFFS_COLL_CUMULANT)
+        return fail(c, LBFFS_E_ARG, "lbffs_create: the cumulant operator is D3Q27 only");
+    if (d.sgs != LBFFS_SGS_SMAGORINSKY && d.sgs != LBFFS_SGS_WALE) return fail(c, LBFFS_E_ARG, "lbffs_create: bad sgs");
+    if (d.wall != LBFFS_WALL_BB && d.wall != LBFFS_WALL_IBB) return fail(c, LBFFS_E_ARG, "lbffs_create: bad wall");
+    if (!(d.cs > 0.f)) return fail(c, LBFFS_E_ARG, "lbffs_create: cs must be > 0");
+    const long long E = (long long)d.nx * d.ny * d.nz;
+    if (E >= (1LL << 32)) return fail(c, LBFFS_E_ARG, "lbffs_create: more than 2^32 - 1 cells");
+
+    c = new lbffs_ctx();
+    c->d = d;
+    c->Q = d.q;
+    c->E = E;
+    c->tsize = d.storage == LBFFS_FP32 ? 4 : 2;
+    cudaError_t e = cudaSetDevice(d.device);
+    if (e != cudaSuccess) {
+        int r = fail(c, LBFFS_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        lbffs_destroy(c);
+        return r;
+    }
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d.device);
+    c->nsm = nsm > 0 ? nsm : 1;
+#define CKC(call)                                                                                          \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess) {                                                                           \
+            int r_ = fail(c, LBFFS_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+            g_thread_error = c->err;                                                                       \
+            lbffs_destroy(c);                                                                              \
+            return r_;                                                                                     \
+        }                                                                                                  \
+    } while (0)
+    CKC(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    const size_t qe = (size_t)c->Q * (size_t)E;
+    for (int b = 0; b < 2; b++) {
+        CKC(cudaMalloc(&c->f[b], qe * c->tsize + 16));
+        CKC(cudaMemset(c->f[b], 0, qe * c->tsize + 16));
+    }
+    for (int b = 0; b < 4; b++) CKC(dalloc(&c->iarr[b], E));
+    CKC(dalloc(&c->solid, E));
+    CKC(dalloc(&c->nei, E));
+    CKC(dalloc(&c->flags, E));
+    CKC(dalloc(&c->bc, E));
+    CKC(dalloc(&c->u0, E));
+    CKC(dalloc(&c->v0, E));
+    CKC(dalloc(&c->w0, E));
+    CKC(dalloc(&c->omega, E));
+    CKC(dalloc(&c->sdf, E));
+    for (auto& row : c->macro)
+        for (float*& p : row) CKC(dalloc(&p, E));
+    for (int a = 0; a < 3; a++) {
+        CKC(dalloc(&c->fw[a], E));
+        CKC(dalloc(&c->g[a], E));
+    }
+    CKC(dalloc(&c->d_err, 1));
+    c->stage_elems = (size_t)16 << 20;  // 64 MB float staging for population conversion
+    if (c->stage_elems > qe) c->stage_elems = qe;
+    CKC(dalloc(&c->stage, c->stage_elems));
+    c->partial_blocks = 4 * c->nsm;
+    CKC(dalloc(&c->partial, (size_t)3 * c->partial_blocks));
+    CKC(fill_f32(c->sdf, 10000.f, E, c->stream));
+    CKC(fill_f32(c->omega, 1.f, E, c->stream));
+    CKC(cudaStreamSynchronize(c->stream));
+#undef CKC
+    *out = c;
+    return LBFFS_OK;
+}
+
+static int commit(lbffs_ctx* c)
+{
+    const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
+    const long long E = c->E;
+    // validate boundary codes (WallFunction, code 7, is not built)
+    std::vector<int> codes(E);
+    for (int b = 1; b <= 3; b++) {
+        CK(cudaMemcpyAsync(codes.data(), c->iarr[b], sizeof(int) * E, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (long long i = 0; i < E; i++) {
+            const int v = codes[i];
+            if (v == BC_WALLFN)
+                return fail(c, LBFFS_E_UNSUPPORTED, "boundary code 7 (WallFunction) is not supported");
+            if (!(v == 0 || v == 1 || v == 3 || v == 4 || v == 5 || v == 6))
+                return fail(c, LBFFS_E_ARG, "invalid boundary code " + std::to_string(v));
+        }
+        // sponge zone face-centre codes (tauSpongeZone, kernel.cl:2447-2501)
+        const long long cen[2] = {b == 1   ? ((long long)(nz / 2) * ny + ny / 2) * nx + 0
+                                  : b == 2 ? ((long long)(nz / 2) * ny + 0) * nx + nx / 2
+                                           : ((long long)0 * ny + ny / 2) * nx + nx / 2,
+                                  b == 1   ? ((long long)(nz / 2) * ny + ny / 2) * nx + nx - 1
+                                  : b == 2 ? ((long long)(nz / 2) * ny + ny - 1) * nx + nx / 2
+                                           : ((long long)(nz - 1) * ny + ny / 2) * nx + nx / 2};
+        for (int s = 0; s < 2; s++) {
+            const int v = codes[cen[s]];
+            const int bit = 2 * (b - 1) + s;
+            if (v == BC_OUTLET || v == BC_FIXDEN) c->sponge_mask |= (1 << bit);
+            else c->sponge_mask &= ~(1 << bit);
+        }
+    }
+    // uniform relaxation rate: the value at the domain centre
+    const long long centre = ((long long)(nz / 2) * ny + ny / 2) * nx + nx / 2;
+    CK(cudaMemcpyAsync(&c->omega0, c->omega + centre, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+
+    CK(setup_pack_bc(c->iarr[0], c->iarr[1], c->iarr[2], c->iarr[3], c->bc, nx, ny, nz, c->stream));
+    uint8_t* scratch = nullptr;
+    CK(cudaMalloc(&scratch, E));
+    cudaError_t e = setup_classify(c->Q, c->bc, c->solid, c->nei, c->sdf, c->omega, c->omega0, c->d.cs, c->flags,
+                                   scratch, nx, ny, nz, c->stream);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(scratch);
+    CK(e);
+
+    const long long nb = (E + SETUP_CHUNK - 1) / SETUP_CHUNK;
+    unsigned* d_counts = nullptr;
+    unsigned long long* d_off = nullptr;
+    CK(cudaMalloc(&d_counts, sizeof(unsigned) * nb));
+    e = setup_count_special(c->flags, E, d_counts, c->stream);
+    std::vector<unsigned> counts(nb);
+    std::vector<unsigned long long> off(nb);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(counts.data(), d_counts, sizeof(unsigned) * nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    unsigned long long total = 0;
+    for (long long b = 0; b < nb; b++) {
+        off[b] = total;
+        total += counts[b];
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(unsigned long long) * nb);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_off, off.data(), sizeof(unsigned long long) * nb, cudaMemcpyHostToDevice, c->stream);
+    if (c->special) {
+        cudaFree(c->special);
+        c->special = nullptr;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c->special, sizeof(uint32_t) * (total + 1));
+    if (e == cudaSuccess) e = setup_scatter_special(c->flags, E, d_off, c->special, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_counts);
+    if (d_off) cudaFree(d_off);
+    CK(e);
+    c->n_special = (long long)total;
+
+    // per-class counts and zeroed link forces
+    std::vector<uint8_t> fl(E);
+    CK(cudaMemcpyAsync(fl.data(), c->flags, E, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    long long nf = 0, ns = 0, nl = 0, nst = 0;
+    for (long long i = 0; i < E; i++) {
+        const uint8_t v = fl[i];
+        if (v & FL_SOLID) continue;
+        nf++;
+        ns += (v & FL_SPECIAL) != 0;
+        nl += (v & FL_LINK) != 0;
+        nst += (v & FL_STORE) != 0;
+    }
+    c->counts[0] = nf;
+    c->counts[1] = ns;
+    c->counts[2] = nl;
+    c->counts[3] = nst;
+    for (int a = 0; a < 3; a++) CK(cudaMemsetAsync(c->fw[a], 0, sizeof(float) * E, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->dirty = false;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t bytes)
+{
+    if (!c || !host) return fail(c, LBFFS_E_ARG, "lbffs_upload: null argument");
+    if (field < 0 || field >= LBFFS_NFIELDS) return fail(c, LBFFS_E_ARG, "lbffs_upload: bad field id");
+    if (bytes != field_bytes(c, field))
+        return fail(c, LBFFS_E_ARG, "lbffs_upload: field " + std::to_string(field) + " expects " +
+                                         std::to_string(field_bytes(c, field)) + " bytes, got " + std::to_string(bytes));
+    CK(cudaSetDevice(c->d.device));
+    FieldInfo fi = field_info(field);
+    if (fi.kind == K_F) {
+        const size_t total = (size_t)c->Q * (size_t)c->E;
+        const float* h = static_cast<const float*>(host);
+        for (size_t s = 0; s < total; s += c->stage_elems) {
+            const size_t n = (total - s < c->stage_elems) ? total - s : c->stage_elems;
+            CK(cudaMemcpyAsync(c->stage, h + s, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+            CK(encode_f(c->d.storage, c->Q, c->stage, c->f[c->fcur], (long long)s, (long long)n, c->E, c->stream));
+        }
+        CK(cudaStreamSynchronize(c->stream));
+        return LBFFS_OK;
+    }
+    if (fi.kind == K_MACRO) {
+        for (int b = 0; b < 2; b++)
+            CK(cudaMemcpyAsync(c->macro[b][fi.macro], host, bytes, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return LBFFS_OK;
+    }
+    void* p = field_ptr(c, field);
+    CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (geometry_field(field)) c->dirty = true;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_download(lbffs_ctx* c, int field, void* host, size_t bytes)
+{
+    if (!c || !host) return fail(c, LBFFS_E_ARG, "lbffs_download: null argument");
+    if (field < 0 || field >= LBFFS_NFIELDS) return fail(c, LBFFS_E_ARG, "lbffs_download: bad field id");
+    if (bytes != field_bytes(c, field)) return fail(c, LBFFS_E_ARG, "lbffs_download: size mismatch");
+    CK(cudaSetDevice(c->d.device));
+    FieldInfo fi = field_info(field);
+    if (fi.kind == K_F) {
+        const size_t total = (size_t)c->Q * (size_t)c->E;
+        float* h = static_cast<float*>(host);
+        for (size_t s = 0; s < total; s += c->stage_elems) {
+            const size_t n = (total - s < c->stage_elems) ? total - s : c->stage_elems;
+            CK(decode_f(c->d.storage, c->Q, c->f[c->fcur], c->stage, (long long)s, (long long)n, c->E, c->stream));
+            CK(cudaMemcpyAsync(h + s, c->stage, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+        }
+        return LBFFS_OK;
+    }
+    const void* p = fi.kind == K_MACRO ? c->macro[c->mcur][fi.macro] : field_ptr(c, field);
+    CK(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return LBFFS_OK;
+}
+
+static cudaEvent_t get_event(lbffs_ctx* c)
+{
+    if (!c->pool.empty()) {
+        cudaEvent_t e = c->pool.back();
+        c->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+static void harvest_timing(lbffs_ctx* c)
+{
+    for (auto& ev : c->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ev.a, ev.b) == cudaSuccess) {
+            c->ms[ev.kind] += ms;
+            c->launches[ev.kind] += 1;
+        }
+        c->pool.push_back(ev.a);
+        c->pool.push_back(ev.b);
+    }
+    c->pending.clear();
+}
+
+extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
+{
+    if (!c || !p) return fail(c, LBFFS_E_ARG, "lbffs_step: null argument");
+    if (nsteps < 0) return fail(c, LBFFS_E_ARG, "lbffs_step: nsteps < 0");
+    CK(cudaSetDevice(c->d.device));
+    if (c->dirty) {
+        int r = commit(c);
+        if (r != LBFFS_OK) return r;
+    }
+    StepArgs a{};
+    a.flags = c->flags;
+    a.bc = c->bc;
+    a.solid = c->solid;
+    a.nei_solid = c->nei;
+    a.u0 = c->u0;
+    a.v0 = c->v0;
+    a.w0 = c->w0;
+    a.omega = c->omega;
+    a.sdf = c->sdf;
+    a.fwx = c->fw[0];
+    a.fwy = c->fw[1];
+    a.fwz = c->fw[2];
+    a.gx = c->g[0];
+    a.gy = c->g[1];
+    a.gz = c->g[2];
+    a.special = c->special;
+    a.n_special = c->n_special;
+    a.E = c->E;
+    a.nx = c->d.nx;
+    a.ny = c->d.ny;
+    a.nz = c->d.nz;
+    a.omega0 = c->omega0;
+    a.dpdx = p->dpdx;
+    a.les = p->les;
+    a.omega_b = p->omega_b;
+    a.spz = p->spz_width;
+    a.clim = p->clim;
+    a.cs = c->d.cs;
+    a.sponge_mask = c->sponge_mask;
+    a.sgs = c->d.sgs;
+    a.wall = c->d.wall;
+    a.ibm_box = c->n_markers > 1 ? c->ibm_box : nullptr;
+    a.err = c->d_err;
+    StepConfig cfg{c->d.storage, c->d.collision, c->d.sgs, c->d.wall,
+                   c->d.sgs == LBFFS_SGS_SMAGORINSKY && p->les != 0.f};
+    auto launch = (c->Q == 19) ? launch_q19 : launch_q27;
+    for (int s = 0; s < nsteps; s++) {
+        a.f_in = c->f[c->fcur];
+        a.f_out = c->f[1 - c->fcur];
+        float** mp = c->macro[c->mcur];
+        float** mn = c->macro[1 - c->mcur];
+        a.rho_p = mp[0];
+        a.u_p = mp[1];
+        a.v_p = mp[2];
+        a.w_p = mp[3];
+        a.tau_p = mp[4];
+        a.rho_n = mn[0];
+        a.u_n = mn[1];
+        a.v_n = mn[2];
+        a.w_n = mn[3];
+        a.tau_n = mn[4];
+        a.store_all = (p->store_fields == 2) || (p->store_fields == 1 && s == nsteps - 1);
+        for (int half = 0; half < 2; half++) {
+            const bool bulk = half == 0;
+            if (!bulk && c->n_special == 0) continue;
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (c->timing) {
+                e0 = get_event(c);
+                e1 = get_event(c);
+                cudaEventRecord(e0, c->stream);
+            }
+            cudaError_t e = launch(a, cfg, bulk, c->stream);
+            if (c->timing) {
+                cudaEventRecord(e1, c->stream);
+                c->pending.push_back({e0, e1, bulk ? 0 : 1});
+            }
+            if (e != cudaSuccess) return fail(c, LBFFS_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+        }
+        if (c->n_markers > 1) {
+            IbmArgs ia{};
+            ia.markers = c->markers;
+            ia.gm = c->gm;
+            ia.acc = c->ibm_acc;
+            ia.lag = c->ibm_lag;
+            ia.box = c->ibm_box;
+            ia.t = c->ibm_t;
+            ia.motion = c->motion;
+            ia.n = c->n_markers;
+            ia.nx = a.nx;
+            ia.ny = a.ny;
+            ia.nz = a.nz;
+            ia.E = c->E;
+            ia.u = mn[1];
+            ia.v = mn[2];
+            ia.w = mn[3];
+            ia.rho = mn[0];
+            ia.flags = c->flags;
+            ia.f_out = a.f_out;
+            ia.gx = c->g[0];
+            ia.gy = c->g[1];
+            ia.gz = c->g[2];
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (c->timing) {
+                e0 = get_event(c);
+                e1 = get_event(c);
+                cudaEventRecord(e0, c->stream);
+            }
+            cudaError_t e = ibm_substep(ia, c->d.storage, c->Q, c->nsm, c->stream);
+            if (c->timing) {
+                cudaEventRecord(e1, c->stream);
+                c->pending.push_back({e0, e1, 2});
+            }
+            if (e != cudaSuccess) return fail(c, LBFFS_E_CUDA, std::string("ibm launch: ") + cudaGetErrorString(e));
+        }
+        c->fcur = 1 - c->fcur;
+        c->mcur = 1 - c->mcur;
+    }
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_synchronize(lbffs_ctx* c)
+{
+    if (!c) return fail(c, LBFFS_E_ARG, "lbffs_synchronize: null context");
+    CK(cudaSetDevice(c->d.device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->timing) harvest_timing(c);
+    int h = 0;
+    CK(cudaMemcpy(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) return fail(c, LBFFS_E_NONFINITE, "non-finite density produced by the step (divergence)");
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_force_sum(lbffs_ctx* c, double out[3])
+{
+    if (!c || !out) return fail(c, LBFFS_E_ARG, "lbffs_force_sum: null argument");
+    CK(cudaSetDevice(c->d.device));
+    out[0] = out[1] = out[2] = 0.0;
+    if (c->dirty || c->n_special == 0) return LBFFS_OK;
+    const int nb = c->partial_blocks;
+    CK(reduce_force(c->special, c->n_special, c->fw[0], c->fw[1], c->fw[2], c->partial, nb, c->stream));
+    std::vector<double> h((size_t)3 * nb);
+    CK(cudaMemcpyAsync(h.data(), c->partial, sizeof(double) * 3 * nb, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int b = 0; b < nb; b++)
+        for (int a = 0; a < 3; a++) out[a] += h[(size_t)3 * b + a];
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_mass(lbffs_ctx* c, double* out)
+{
+    if (!c || !out) return fail(c, LBFFS_E_ARG, "lbffs_mass: null argument");
+    CK(cudaSetDevice(c->d.device));
+    if (c->dirty) {
+        int r = commit(c);
+        if (r != LBFFS_OK) return r;
+    }
+    const int nb = c->partial_blocks;
+    CK(reduce_mass(c->d.storage, c->Q, c->f[c->fcur], c->flags, c->E, c->partial, nb, c->stream));
+    std::vector<double> h(nb);
+    CK(cudaMemcpyAsync(h.data(), c->partial, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double s = 0.0;
+    for (int b = 0; b < nb; b++) s += h[b];
+    *out = s;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_links(lbffs_ctx* c, long long* cells, unsigned* masks, long long capacity, long long* n)
+{
+    if (!c || !n) return fail(c, LBFFS_E_ARG, "lbffs_links: null argument");
+    CK(cudaSetDevice(c->d.device));
+    if (c->dirty) {
+        int r = commit(c);
+        if (r != LBFFS_OK) return r;
+    }
+    *n = 0;
+    if (c->n_special == 0) return LBFFS_OK;
+    uint32_t* d_masks = nullptr;
+    CK(cudaMalloc(&d_masks, sizeof(uint32_t) * c->n_special));
+    cudaError_t e = setup_link_masks(c->Q, c->special, c->n_special, c->bc, c->solid, c->nei, c->d.nx, c->d.ny,
+                                     c->d.nz, d_masks, c->stream);
+    std::vector<uint32_t> hm(c->n_special), hc(c->n_special);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hm.data(), d_masks, sizeof(uint32_t) * c->n_special, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hc.data(), c->special, sizeof(uint32_t) * c->n_special, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_masks);
+    CK(e);
+    long long k = 0;
+    for (long long t = 0; t < c->n_special; t++) {
+        if (!hm[t]) continue;
+        if (k < capacity && cells && masks) {
+            cells[k] = hc[t];
+            masks[k] = hm[t];
+        }
+        k++;
+    }
+    *n = k;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_set_markers(lbffs_ctx* c, const float* xyz, int n)
+{
+    if (!c || (n > 0 && !xyz) || n < 0) return fail(c, LBFFS_E_ARG, "lbffs_set_markers: bad argument");
+    CK(cudaSetDevice(c->d.device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->markers) cudaFree(c->markers);
+    if (c->gm) cudaFree(c->gm);
+    c->markers = nullptr;
+    c->gm = nullptr;
+    c->n_markers = n;
+    if (n == 0) return LBFFS_OK;
+    CK(dalloc(&c->markers, (size_t)3 * n));
+    CK(dalloc(&c->gm, (size_t)3 * n));
+    CK(cudaMemcpy(c->markers, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+    if (!c->ibm_acc) CK(dalloc(&c->ibm_acc, (size_t)3 * c->E));
+    if (!c->ibm_lag) CK(dalloc(&c->ibm_lag, 3));
+    if (!c->ibm_box) CK(dalloc(&c->ibm_box, 12));
+    if (!c->ibm_t) CK(dalloc(&c->ibm_t, 1));
+    IbmArgs ia{};
+    ia.markers = c->markers;
+    ia.box = c->ibm_box;
+    ia.t = c->ibm_t;
+    ia.n = n;
+    ia.nx = c->d.nx;
+    ia.ny = c->d.ny;
+    ia.nz = c->d.nz;
+    CK(ibm_init_box(ia, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_get_markers(lbffs_ctx* c, float* xyz, int n)
+{
+    if (!c || !xyz || n != c->n_markers) return fail(c, LBFFS_E_ARG, "lbffs_get_markers: bad argument");
+    if (n == 0) return LBFFS_OK;
+    CK(cudaSetDevice(c->d.device));
+    CK(cudaMemcpyAsync(xyz, c->markers, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_set_motion(lbffs_ctx* c, const lbffs_motion* m)
+{
+    if (!c || !m) return fail(c, LBFFS_E_ARG, "lbffs_set_motion: null argument");
+    c->motion.trans[0] = m->u_trans;
+    c->motion.trans[1] = m->v_trans;
+    c->motion.trans[2] = m->w_trans;
+    c->motion.rot[0] = m->rot_x;
+    c->motion.rot[1] = m->rot_y;
+    c->motion.rot[2] = m->rot_z;
+    c->motion.axis[0] = m->axis_x;
+    c->motion.axis[1] = m->axis_y;
+    c->motion.axis[2] = m->axis_z;
+    c->motion.rot_omega = m->rot_omega;
+    c->motion.amp[0] = m->amp_x;
+    c->motion.amp[1] = m->amp_y;
+    c->motion.amp[2] = m->amp_z;
+    c->motion.period = m->period;
+    if (c->ibm_t) {
+        CK(cudaSetDevice(c->d.device));
+        CK(cudaMemsetAsync(c->ibm_t, 0, sizeof(long long), c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_ibm_force_sum(lbffs_ctx* c, double out[3])
+{
+    if (!c || !out) return fail(c, LBFFS_E_ARG, "lbffs_ibm_force_sum: null argument");
+    out[0] = out[1] = out[2] = 0.0;
+    if (!c->ibm_lag) return LBFFS_OK;
+    CK(cudaSetDevice(c->d.device));
+    CK(cudaMemcpyAsync(out, c->ibm_lag, sizeof(double) * 3, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->ibm_lag, 0, sizeof(double) * 3, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_get_stream(lbffs_ctx* c, void** stream)
+{
+    if (!c || !stream) return fail(c, LBFFS_E_ARG, "lbffs_get_stream: null argument");
+    *stream = (void*)c->stream;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_set_timing(lbffs_ctx* c, int enabled)
+{
+    if (!c) return fail(c, LBFFS_E_ARG, "lbffs_set_timing: null context");
+    CK(cudaSetDevice(c->d.device));
+    CK(cudaStreamSynchronize(c->stream));
+    harvest_timing(c);
+    c->timing = enabled != 0;
+    for (int k = 0; k < 3; k++) {
+        c->ms[k] = 0;
+        c->launches[k] = 0;
+    }
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_kernel_time(lbffs_ctx* c, const char* name, double* total_ms, long long* launches)
+{
+    if (!c || !name || !total_ms || !launches) return fail(c, LBFFS_E_ARG, "lbffs_kernel_time: null argument");
+    int k = !strcmp(name, "bulk") ? 0 : !strcmp(name, "special") ? 1 : !strcmp(name, "ibm") ? 2 : -1;
+    if (k < 0) return fail(c, LBFFS_E_ARG, "lbffs_kernel_time: unknown kernel name");
+    CK(cudaSetDevice(c->d.device));
+    CK(cudaStreamSynchronize(c->stream));
+    harvest_timing(c);
+    *total_ms = c->ms[k];
+    *launches = c->launches[k];
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_cell_counts(lbffs_ctx* c, long long out[4])
+{
+    if (!c || !out) return fail(c, LBFFS_E_ARG, "lbffs_cell_counts: null argument");
+    CK(cudaSetDevice(c->d.device));
+    if (c->dirty) {
+        int r = commit(c);
+        if (r != LBFFS_OK) return r;
+    }
+    for (int k = 0; k < 4; k++) out[k] = c->counts[k];
+    return LBFFS_OK;
+}

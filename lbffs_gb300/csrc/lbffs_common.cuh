@@ -1,0 +1,172 @@
+// Shared device definitions of the GB300 LBFFS step: lattice tables, population
+// storage codecs, per-cell flag bits and the kernel argument block.
+//
+// Data layout in HBM (one context = one lattice):
+//   populations   f[q*E + ic], ic = (k*ny + j)*nx + i, two copies (pull ping-pong),
+//                 each element float (FP32), or a shifted/scaled half / bfloat16
+//   flags         u8 per cell (FL_* bits below), built on the device from the
+//                 reference's boundary/solid/neiSolid/sdf/omega arrays
+//   bc            u16 per cell: boundary1 | boundary2<<3 | boundary3<<6 | face<<9
+//   macroscopics  rho,u,v,w,tauSGS, two copies (previous step / this step); only
+//                 cells whose values are read later are written each step
+//   special list  u32 indices of domain-face and STL-link cells, which take the
+//                 general boundary path; every other fluid cell takes the lean
+//                 bulk path (19 or 27 loads, collision, 19 or 27 stores)
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lbffs {
+
+// Boundary codes: src/input.hpp:221-256
+enum BcCode { BC_CYCLIC = 0, BC_BB = 1, BC_OUTLET = 3, BC_SYM = 4, BC_FIXVEL = 5, BC_FIXDEN = 6, BC_WALLFN = 7 };
+enum Storage { ST_FP32 = 0, ST_FP16S = 1, ST_BF16S = 2 };
+enum Collision { COLL_RR = 0, COLL_CUMULANT = 1 };
+enum Sgs { SGS_SMAG = 0, SGS_WALE = 1 };
+enum Wall { WALL_BB = 0, WALL_IBB = 1 };
+
+// Cell flags
+constexpr uint8_t FL_SOLID = 1;    // solid cell: skipped (kernel.cl:3549)
+constexpr uint8_t FL_SPECIAL = 2;  // domain-face or STL-link cell: general path
+constexpr uint8_t FL_STORE = 4;    // macroscopics are read by a neighbour next step: store them
+constexpr uint8_t FL_SDF = 8;      // near-wall damping factor < 1: read sdf
+constexpr uint8_t FL_OMEGA = 16;   // omega differs from the uniform omega0: read omega[]
+constexpr uint8_t FL_LINK = 32;    // has at least one STL link
+constexpr uint8_t FL_FACE = 64;    // on the domain border
+
+constexpr float FP16S_SCALE = 32768.0f;  // (f - w) * 2^15 keeps |f - w| < 2 in range, 1.9e-9 above subnormals
+constexpr float FP16S_INV = 1.0f / 32768.0f;
+
+// ---- lattice tables (reference order: D3Q19 kernel.cl:3555-3560, D3Q27 kernel.cl:2742-2747) ----
+__host__ __device__ constexpr int lat_c(int Q, int q, int a)
+{
+    constexpr int c19[19][3] = {{0, 0, 0},  {1, 0, 0},   {-1, 0, 0}, {0, 1, 0},  {0, -1, 0}, {0, 0, 1},   {0, 0, -1},
+                                {1, 1, 0},  {-1, -1, 0}, {1, -1, 0}, {-1, 1, 0}, {1, 0, 1},  {-1, 0, -1}, {1, 0, -1},
+                                {-1, 0, 1}, {0, 1, 1},   {0, -1, -1}, {0, 1, -1}, {0, -1, 1}};
+    constexpr int c27[27][3] = {{0, 0, 0},   {1, 0, 0},   {-1, 0, 0},  {0, 1, 0},   {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
+                                {1, 1, 0},   {-1, -1, 0}, {1, -1, 0},  {-1, 1, 0},  {1, 0, 1},  {-1, 0, -1}, {1, 0, -1},
+                                {-1, 0, 1},  {0, 1, 1},   {0, -1, -1}, {0, 1, -1},  {0, -1, 1}, {1, 1, 1},  {-1, -1, -1},
+                                {-1, 1, 1},  {1, -1, -1}, {1, -1, 1},  {-1, 1, -1}, {1, 1, -1}, {-1, -1, 1}};
+    return Q == 19 ? c19[q][a] : c27[q][a];
+}
+
+__host__ __device__ constexpr int lat_n2(int Q, int q)
+{
+    return lat_c(Q, q, 0) * lat_c(Q, q, 0) + lat_c(Q, q, 1) * lat_c(Q, q, 1) + lat_c(Q, q, 2) * lat_c(Q, q, 2);
+}
+
+__host__ __device__ constexpr float lat_w(int Q, int q)
+{
+    return Q == 19 ? (lat_n2(Q, q) == 0 ? 1.0f / 3.0f : lat_n2(Q, q) == 1 ? 1.0f / 18.0f : 1.0f / 36.0f)
+                   : (lat_n2(Q, q) == 0   ? float(8.0 / 27.0)
+                      : lat_n2(Q, q) == 1 ? float(2.0 / 27.0)
+                      : lat_n2(Q, q) == 2 ? float(1.0 / 54.0)
+                                          : float(1.0 / 216.0));
+}
+
+__host__ __device__ constexpr int lat_find(int Q, int x, int y, int z)
+{
+    for (int q = 0; q < Q; q++)
+        if (lat_c(Q, q, 0) == x && lat_c(Q, q, 1) == y && lat_c(Q, q, 2) == z) return q;
+    return -1;
+}
+
+__host__ __device__ constexpr int lat_opp(int Q, int q)
+{
+    return lat_find(Q, -lat_c(Q, q, 0), -lat_c(Q, q, 1), -lat_c(Q, q, 2));
+}
+
+// ---- population storage codecs ----
+template <int S>
+struct Codec;
+
+template <>
+struct Codec<ST_FP32> {
+    using T = float;
+    static __device__ __forceinline__ float load(const T* p, float) { return __ldg(p); }
+    static __device__ __forceinline__ void store(T* p, float v, float) { __stcs(p, v); }
+    static __host__ __device__ float to_float(T h, float) { return h; }
+};
+
+// FP16S: IEEE half of (f - w_q) * 2^15; arithmetic stays FP32.
+template <>
+struct Codec<ST_FP16S> {
+    using T = __half;
+    static __device__ __forceinline__ float load(const T* p, float w)
+    {
+        return fmaf(__half2float(__ldg(p)), FP16S_INV, w);
+    }
+    static __device__ __forceinline__ void store(T* p, float v, float w)
+    {
+        *p = __float2half_rn((v - w) * FP16S_SCALE);
+    }
+};
+
+// BF16S: bfloat16 of (f - w_q); arithmetic stays FP32.
+template <>
+struct Codec<ST_BF16S> {
+    using T = __nv_bfloat16;
+    static __device__ __forceinline__ float load(const T* p, float w) { return __bfloat162float(__ldg(p)) + w; }
+    static __device__ __forceinline__ void store(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
+};
+
+// ---- kernel argument block ----
+struct StepArgs {
+    const void* f_in;
+    void* f_out;
+    const uint8_t* flags;
+    const uint16_t* bc;
+    const uint8_t* solid;
+    const uint8_t* nei_solid;
+    const float *u0, *v0, *w0, *omega, *sdf;
+    const float *rho_p, *u_p, *v_p, *w_p, *tau_p;  // previous step
+    float *rho_n, *u_n, *v_n, *w_n, *tau_n;        // this step
+    float *fwx, *fwy, *fwz;
+    float *gx, *gy, *gz;
+    const uint32_t* special;
+    long long n_special;
+    long long E;
+    int nx, ny, nz;
+    float omega0, dpdx, les, omega_b, spz, clim, cs;
+    int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity
+    int store_all;    // store rho/u/v/w/tau for every fluid cell this step
+    int sgs, wall;    // Sgs / Wall selections (runtime in the boundary kernel)
+    const int* ibm_box;  // device int[6] lo/hi of the marker box (cells inside store macroscopics), or null
+    int* err;            // device error word (non-finite density seen), may be null
+};
+
+__device__ __forceinline__ bool in_box(const StepArgs& a, int i, int j, int k)
+{
+    if (!a.ibm_box) return false;
+    const int* b = a.ibm_box;
+    return i >= b[0] && i <= b[3] && j >= b[1] && j <= b[4] && k >= b[2] && k <= b[5];
+}
+
+// tauSpongeZone (D3Q19 kernel.cl:2444-2503)
+__device__ __forceinline__ float sponge_tau(const StepArgs& a, float tau, float tsgs, int i, int j, int k)
+{
+    if (a.sponge_mask == 0) return tau;
+    const int x[3] = {i, j, k};
+    const int N[3] = {a.nx, a.ny, a.nz};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const float n = (float)N[d];
+        if ((a.sponge_mask >> (2 * d)) & 1) {
+            if ((float)x[d] < n * a.spz) {
+                const float fx = (float)x[d] / (n * a.spz);
+                tau = (1.f - fx) * (1.f - tsgs) + fx * tau;
+            }
+        }
+        if ((a.sponge_mask >> (2 * d + 1)) & 1) {
+            if ((float)x[d] > n * (1.f - a.spz)) {
+                const float fx = (float)(N[d] - x[d]) / (n * a.spz);
+                tau = (1.f - fx) * (1.f - tsgs) + fx * tau;
+            }
+        }
+    }
+    return tau;
+}
+
+}  // namespace lbffs

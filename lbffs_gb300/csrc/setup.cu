@@ -1,0 +1,350 @@
+// Geometry commit, population format conversion and FP64 reductions.
+//
+// The reference hands the device one int32 array per boundary code and u8 solid /
+// neiSolid arrays (D3Q19_opencl/ns.cpp:405-436).  Here they are condensed once per
+// geometry change into a u16 boundary word and a u8 flag per cell plus a compact list
+// of the cells that need the general boundary path; the time step never touches the
+// int32 arrays again.
+#include "launch.h"
+#include "step_kernels.cuh"
+
+namespace lbffs {
+
+__global__ void k_pack_bc(const int* boundary, const int* b1, const int* b2, const int* b3, uint16_t* bc, int nx,
+                          int ny, int nz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx) return;
+    const long long ic = ((long long)blockIdx.z * ny + blockIdx.y) * nx + i;
+    bc[ic] = (uint16_t)((b1[ic] & 7) | ((b2[ic] & 7) << 3) | ((b3[ic] & 7) << 6) | ((boundary[ic] == 1) << 9));
+}
+
+cudaError_t setup_pack_bc(const int* boundary, const int* b1, const int* b2, const int* b3, uint16_t* bc, int nx,
+                          int ny, int nz, cudaStream_t st)
+{
+    k_pack_bc<<<dim3((nx + 127) / 128, ny, nz), 128, 0, st>>>(boundary, b1, b2, b3, bc, nx, ny, nz);
+    return cudaGetLastError();
+}
+
+// pass 1: solid / face / link / special bits
+template <int Q>
+__global__ void k_classify1(const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, uint8_t* flags, int nx,
+                            int ny, int nz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const long long ic = ((long long)k * ny + j) * nx + i;
+    if (solid[ic]) {
+        flags[ic] = FL_SOLID;
+        return;
+    }
+    const uint16_t bw = bc[ic];
+    const int b[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
+    const bool face = (bw >> 9) & 1;
+    const bool border = i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (nz > 1 && (k == 0 || k == nz - 1));
+    bool link = false;
+    if (nei[ic] == 1) {
+        const int x[3] = {i, j, k}, N[3] = {nx, ny, nz};
+#pragma unroll
+        for (int q = 1; q < Q; q++) {
+            const long long up = upwind<Q>(q, x, N, b, face);
+            link |= (up >= 0 && solid[up] == 1);
+        }
+    }
+    uint8_t fl = 0;
+    if (face || border) fl |= FL_FACE;
+    if (link) fl |= FL_LINK;
+    if (face || border || link) fl |= FL_SPECIAL;
+    flags[ic] = fl;
+}
+
+// pass 2: cells next to a special cell store their macroscopics; damping / omega read bits
+__global__ void k_classify2(const uint8_t* pass1, uint8_t* flags, const float* sdf, const float* omega, float omega0,
+                            float cs, int nx, int ny, int nz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const long long ic = ((long long)k * ny + j) * nx + i;
+    uint8_t fl = pass1[ic];
+    if (fl & FL_SOLID) {
+        flags[ic] = fl;
+        return;
+    }
+    bool near = false;
+    for (int dk = -1; dk <= 1; dk++)
+        for (int dj = -1; dj <= 1; dj++)
+            for (int di = -1; di <= 1; di++) {
+                int ii = i + di, jj = j + dj, kk = k + dk;
+                if (ii < 0) ii += nx;
+                if (ii >= nx) ii -= nx;
+                if (jj < 0) jj += ny;
+                if (jj >= ny) jj -= ny;
+                if (kk < 0) kk += nz;
+                if (kk >= nz) kk -= nz;
+                near |= (pass1[((long long)kk * ny + jj) * nx + ii] & FL_SPECIAL) != 0;
+            }
+    fl &= (FL_SPECIAL | FL_LINK | FL_FACE);
+    if (near) fl |= FL_STORE;
+    const float s = sdf[ic];
+    if (s != 10000.f && s > 0.f && 0.41f * s / cs < 1.f) fl |= FL_SDF;
+    if (__float_as_uint(omega[ic]) != __float_as_uint(omega0)) fl |= FL_OMEGA;
+    flags[ic] = fl;
+}
+
+cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
+                           const float* omega, float omega0, float cs, uint8_t* flags, uint8_t* scratch, int nx, int ny,
+                           int nz, cudaStream_t st)
+{
+    const dim3 grid((nx + 127) / 128, ny, nz);
+    if (Q == 19) k_classify1<19><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
+    else k_classify1<27><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_classify2<<<grid, 128, 0, st>>>(scratch, flags, sdf, omega, omega0, cs, nx, ny, nz);
+    return cudaGetLastError();
+}
+
+__global__ void k_count_special(const uint8_t* flags, long long E, unsigned* counts)
+{
+    const long long ic = (long long)blockIdx.x * SETUP_CHUNK + threadIdx.x;
+    const bool sp = ic < E && (flags[ic] & FL_SPECIAL);
+    const int n = __syncthreads_count(sp);
+    if (threadIdx.x == 0) counts[blockIdx.x] = (unsigned)n;
+}
+
+cudaError_t setup_count_special(const uint8_t* flags, long long E, unsigned* counts, cudaStream_t st)
+{
+    const unsigned nb = (unsigned)((E + SETUP_CHUNK - 1) / SETUP_CHUNK);
+    k_count_special<<<nb, SETUP_CHUNK, 0, st>>>(flags, E, counts);
+    return cudaGetLastError();
+}
+
+__global__ void k_scatter_special(const uint8_t* flags, long long E, const unsigned long long* offsets, uint32_t* out)
+{
+    __shared__ unsigned warp_base[SETUP_CHUNK / 32];
+    const long long ic = (long long)blockIdx.x * SETUP_CHUNK + threadIdx.x;
+    const bool sp = ic < E && (flags[ic] & FL_SPECIAL);
+    const unsigned m = __ballot_sync(0xffffffffu, sp);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_base[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned s = 0;
+        for (int w = 0; w < SETUP_CHUNK / 32; w++) {
+            const unsigned c = warp_base[w];
+            warp_base[w] = s;
+            s += c;
+        }
+    }
+    __syncthreads();
+    if (sp) {
+        const unsigned pos = warp_base[warp] + __popc(m & ((1u << lane) - 1u));
+        out[offsets[blockIdx.x] + pos] = (uint32_t)ic;
+    }
+}
+
+cudaError_t setup_scatter_special(const uint8_t* flags, long long E, const unsigned long long* offsets, uint32_t* out,
+                                  cudaStream_t st)
+{
+    const unsigned nb = (unsigned)((E + SETUP_CHUNK - 1) / SETUP_CHUNK);
+    k_scatter_special<<<nb, SETUP_CHUNK, 0, st>>>(flags, E, offsets, out);
+    return cudaGetLastError();
+}
+
+// bit q set: (cell, q) is an STL link, i.e. neiSolid[cell] && solid[upwind(cell, q)] (kernel.cl:1940-1943)
+template <int Q>
+__global__ void k_link_masks(const uint32_t* special, long long n, const uint16_t* bc, const uint8_t* solid,
+                             const uint8_t* nei, int nx, int ny, int nz, uint32_t* masks)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const long long ic = special[t];
+    const int x[3] = {(int)(ic % nx), (int)((ic / nx) % ny), (int)(ic / ((long long)nx * ny))}, N[3] = {nx, ny, nz};
+    const uint16_t bw = bc[ic];
+    const int b[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
+    const bool face = (bw >> 9) & 1;
+    uint32_t m = 0;
+    if (nei[ic] == 1 && !solid[ic]) {
+#pragma unroll
+        for (int q = 1; q < Q; q++) {
+            const long long up = upwind<Q>(q, x, N, b, face);
+            if (up >= 0 && solid[up] == 1) m |= 1u << q;
+        }
+    }
+    masks[t] = m;
+}
+
+cudaError_t setup_link_masks(int Q, const uint32_t* special, long long n, const uint16_t* bc, const uint8_t* solid,
+                             const uint8_t* nei, int nx, int ny, int nz, uint32_t* masks, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const unsigned nb = (unsigned)((n + 127) / 128);
+    if (Q == 19) k_link_masks<19><<<nb, 128, 0, st>>>(special, n, bc, solid, nei, nx, ny, nz, masks);
+    else k_link_masks<27><<<nb, 128, 0, st>>>(special, n, bc, solid, nei, nx, ny, nz, masks);
+    return cudaGetLastError();
+}
+
+// ---- population format conversion (host float32 layout <-> storage) ----
+template <int S, int Q>
+__global__ void k_encode(const float* src, typename Codec<S>::T* dst, long long start, long long count, long long E)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const long long e = start + t;
+    const int q = (int)(e / E);
+    float w = 0.f;
+#pragma unroll
+    for (int p = 0; p < Q; p++)
+        if (p == q) w = lat_w(Q, p);
+    Codec<S>::store(dst + e, src[t], w);
+}
+
+template <int S, int Q>
+__global__ void k_decode(const typename Codec<S>::T* src, float* dst, long long start, long long count, long long E)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const long long e = start + t;
+    const int q = (int)(e / E);
+    float w = 0.f;
+#pragma unroll
+    for (int p = 0; p < Q; p++)
+        if (p == q) w = lat_w(Q, p);
+    dst[t] = Codec<S>::load(src + e, w);
+}
+
+template <int S>
+static cudaError_t enc_q(int Q, const float* src, void* dst, long long start, long long count, long long E, cudaStream_t st)
+{
+    using T = typename Codec<S>::T;
+    const unsigned nb = (unsigned)((count + 255) / 256);
+    if (Q == 19) k_encode<S, 19><<<nb, 256, 0, st>>>(src, static_cast<T*>(dst), start, count, E);
+    else k_encode<S, 27><<<nb, 256, 0, st>>>(src, static_cast<T*>(dst), start, count, E);
+    return cudaGetLastError();
+}
+
+template <int S>
+static cudaError_t dec_q(int Q, const void* src, float* dst, long long start, long long count, long long E, cudaStream_t st)
+{
+    using T = typename Codec<S>::T;
+    const unsigned nb = (unsigned)((count + 255) / 256);
+    if (Q == 19) k_decode<S, 19><<<nb, 256, 0, st>>>(static_cast<const T*>(src), dst, start, count, E);
+    else k_decode<S, 27><<<nb, 256, 0, st>>>(static_cast<const T*>(src), dst, start, count, E);
+    return cudaGetLastError();
+}
+
+cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long start, long long count, long long E,
+                     cudaStream_t st)
+{
+    switch (storage) {
+        case ST_FP32: return cudaMemcpyAsync(static_cast<float*>(dst) + start, src, sizeof(float) * count,
+                                             cudaMemcpyDeviceToDevice, st);
+        case ST_FP16S: return enc_q<ST_FP16S>(Q, src, dst, start, count, E, st);
+        case ST_BF16S: return enc_q<ST_BF16S>(Q, src, dst, start, count, E, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long start, long long count, long long E,
+                     cudaStream_t st)
+{
+    switch (storage) {
+        case ST_FP32: return cudaMemcpyAsync(dst, static_cast<const float*>(src) + start, sizeof(float) * count,
+                                             cudaMemcpyDeviceToDevice, st);
+        case ST_FP16S: return dec_q<ST_FP16S>(Q, src, dst, start, count, E, st);
+        case ST_BF16S: return dec_q<ST_BF16S>(Q, src, dst, start, count, E, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+__global__ void k_fill(float* p, float v, long long n)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = v;
+}
+
+cudaError_t fill_f32(float* p, float v, long long n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_fill<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, v, n);
+    return cudaGetLastError();
+}
+
+// ---- FP64 reductions (per-block partials, summed in a fixed order on the host) ----
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += sh[w];
+    __syncthreads();
+    return s;
+}
+
+__global__ void k_reduce_force(const uint32_t* cells, long long n, const float* fx, const float* fy, const float* fz,
+                               double* partial)
+{
+    __shared__ double sh[REDUCE_BS / 32];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (long long t = (long long)blockIdx.x * REDUCE_BS + threadIdx.x; t < n; t += (long long)gridDim.x * REDUCE_BS) {
+        const long long ic = cells[t];
+        a += (double)fx[ic];
+        b += (double)fy[ic];
+        c += (double)fz[ic];
+    }
+    a = block_sum(a, sh);
+    b = block_sum(b, sh);
+    c = block_sum(c, sh);
+    if (threadIdx.x == 0) {
+        partial[3 * blockIdx.x + 0] = a;
+        partial[3 * blockIdx.x + 1] = b;
+        partial[3 * blockIdx.x + 2] = c;
+    }
+}
+
+cudaError_t reduce_force(const uint32_t* cells, long long n, const float* fx, const float* fy, const float* fz,
+                         double* partial, int nblocks, cudaStream_t st)
+{
+    k_reduce_force<<<nblocks, REDUCE_BS, 0, st>>>(cells, n, fx, fy, fz, partial);
+    return cudaGetLastError();
+}
+
+template <int S, int Q>
+__global__ void k_reduce_mass(const typename Codec<S>::T* f, const uint8_t* flags, long long E, double* partial)
+{
+    __shared__ double sh[REDUCE_BS / 32];
+    double acc = 0.0;
+    for (long long ic = (long long)blockIdx.x * REDUCE_BS + threadIdx.x; ic < E; ic += (long long)gridDim.x * REDUCE_BS) {
+        if (flags[ic] & FL_SOLID) continue;
+        float r = 0.f;
+#pragma unroll
+        for (int q = 0; q < Q; q++) r += Codec<S>::load(f + (long long)q * E + ic, lat_w(Q, q));
+        acc += (double)r;
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+cudaError_t reduce_mass(int storage, int Q, const void* f, const uint8_t* flags, long long E, double* partial,
+                        int nblocks, cudaStream_t st)
+{
+#define LBFFS_MASS(S)                                                                                                  \
+    (Q == 19 ? (k_reduce_mass<S, 19><<<nblocks, REDUCE_BS, 0, st>>>(static_cast<const Codec<S>::T*>(f), flags, E, partial), 0) \
+             : (k_reduce_mass<S, 27><<<nblocks, REDUCE_BS, 0, st>>>(static_cast<const Codec<S>::T*>(f), flags, E, partial), 0))
+    switch (storage) {
+        case ST_FP32: LBFFS_MASS(ST_FP32); break;
+        case ST_FP16S: LBFFS_MASS(ST_FP16S); break;
+        case ST_BF16S: LBFFS_MASS(ST_BF16S); break;
+        default: return cudaErrorInvalidValue;
+    }
+#undef LBFFS_MASS
+    return cudaGetLastError();
+}
+
+}  // namespace lbffs

@@ -33,8 +33,9 @@ The host geometry code (``src/walls.hpp`` / ``src/stl.hpp``) is compiled
 by the same recipe into ``voxel_ref19`` / ``voxel_ref27`` with ``boost_stub/`` standing in for
 the one Boost call it uses.
 
-Usage: ``python oracle/build_ref.py [--jobs N]``.  Exits 0 with a message if
-the reference checkout is absent (nothing to build).
+Usage: ``python oracle/build_ref.py [--jobs N]``.  Without the reference
+checkout (e.g. on a machine the tree was copied to) it compiles the patched
+sources already present in ``oracle/_ref`` and exits 0 if there are none.
 """
 from __future__ import annotations
 
@@ -175,29 +176,36 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     args = ap.parse_args(argv)
-    if not os.path.isdir(os.path.join(REF, "D3Q19_opencl")):
-        print("build_ref: reference checkout not present; nothing to build")
-        return 0
+    have_ref = os.path.isdir(os.path.join(REF, "D3Q19_opencl"))
     os.makedirs(OUT, exist_ok=True)
     variants = []
     for q in (19, 27):
         walls = ("bb", "ibb") if q == 19 else ("ibb",)
         for sgs in ("smag", "wale"):
             for wall in walls:
-                text = patch_kernel(q, sgs, wall)
-                with open(os.path.join(OUT, f"kernel_d3q{q}_{sgs}_{wall}.c"), "w") as fh:
-                    fh.write(text)
+                ksrc = os.path.join(OUT, f"kernel_d3q{q}_{sgs}_{wall}.c")
+                if have_ref:
+                    with open(ksrc, "w") as fh:
+                        fh.write(patch_kernel(q, sgs, wall))
+                elif not os.path.exists(ksrc):
+                    continue
                 for real in ("f32", "f64"):
-                    variants.append((q, sgs, wall, real))
+                    so = os.path.join(OUT, f"libref_d3q{q}_{sgs}_{wall}_{real}.so")
+                    if have_ref or not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(ksrc):
+                        variants.append((q, sgs, wall, real))
+    if not have_ref and not variants:
+        print("build_ref: reference checkout and generated sources absent (or up to date); nothing to build")
+        return 0
     log = []
     with ThreadPoolExecutor(args.jobs) as ex:
         futs = [ex.submit(build_one, *v, log) for v in variants]
-        futs += [ex.submit(build_voxel, q, log) for q in (19, 27)]
+        if have_ref:
+            futs += [ex.submit(build_voxel, q, log) for q in (19, 27)]
         ok = all(f.result() for f in futs)
     if not ok:
         print("\n".join(log), file=sys.stderr)
         return 1
-    print(f"build_ref: built {len(variants)} kernel libraries + voxel_ref into {OUT}")
+    print(f"build_ref: built {len(variants)} kernel libraries into {OUT}")
     return 0
 
 

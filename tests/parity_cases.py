@@ -1,0 +1,92 @@
+"""Small, seeded cases shared by the golden-vector generator and the parity tests.
+
+Each case is built with :mod:`lbffs_gb300.case` / :mod:`lbffs_gb300.geometry`
+exactly as the reference driver would build it (ns.cpp setup), so the same
+arrays can be fed to the reference compiled from source (``oracle/_ref``), to
+the CPU restatement (``oracle/``) and to the CUDA library.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from lbffs_gb300.case import (BOUNCEBACK, CYCLIC, FIXEDDENSITY, FIXEDVELOCITY, OUTLET, SYMMETRY, FaceBC,
+                              cavity_faces, channel_faces, make_case)
+from lbffs_gb300.geometry import backward_step, cylinder_markers, cylinder_z
+
+
+def _mixed_faces():
+    return {"nxMin": FaceBC(FIXEDVELOCITY, 0, 0, 0.04, 0.01, 0.0), "nxMax": FaceBC(OUTLET, 0, 0),
+            "nyMin": FaceBC(0, SYMMETRY, 0), "nyMax": FaceBC(0, FIXEDVELOCITY, 0, 0.03, 0.0, 0.0),
+            "nzMin": FaceBC(0, 0, SYMMETRY), "nzMax": FaceBC(0, 0, BOUNCEBACK)}
+
+
+def _density_faces():
+    f = channel_faces(0.05, top_bottom=BOUNCEBACK, z_periodic=False)
+    f["nxMax"] = FaceBC(FIXEDDENSITY, CYCLIC, CYCLIC)
+    return f
+
+
+def build(name):
+    """Return (case, run) where run holds the solver selections and step keyword arguments."""
+    if name == "cavity_q19":
+        c = make_case(12, 12, 12, 19, cavity_faces(0.05), nu=0.032)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=60, kw={})
+    if name == "cavity_q19_les":
+        c = make_case(12, 12, 12, 19, cavity_faces(0.08), nu=0.002)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=40, kw=dict(LES=1.0))
+    if name == "cavity_q19_wale":
+        c = make_case(12, 12, 12, 19, cavity_faces(0.05), nu=0.01)
+        return c, dict(sgs="wale", wall="bb", collision="rr", steps=40, kw={})
+    if name == "cylinder_q19_ibb_les_sponge":
+        solid, sdf = cylinder_z(32, 20, 6, 10.3, 9.8, 3.6)
+        c = make_case(32, 20, 6, 19, channel_faces(0.05), nu=0.004, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="ibb", collision="rr", steps=40, kw=dict(LES=1.0, spzWidth=0.2))
+    if name == "cylinder_q19_bb":
+        solid, sdf = cylinder_z(32, 20, 6, 10.3, 9.8, 3.6)
+        c = make_case(32, 20, 6, 19, channel_faces(0.05), nu=0.02, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=40, kw={})
+    if name == "cylinder2d_q19_ibb":
+        solid, sdf = cylinder_z(40, 24, 1, 12.4, 11.7, 4.3)
+        c = make_case(40, 24, 1, 19, channel_faces(0.05), nu=0.02, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="ibb", collision="rr", steps=40, kw={})
+    if name == "mixed_q19":
+        c = make_case(16, 14, 12, 19, _mixed_faces(), nu=0.02)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=40, kw={})
+    if name == "density_q19_dpdx":
+        solid, sdf = cylinder_z(28, 18, 8, 9.0, 8.6, 3.1)
+        c = make_case(28, 18, 8, 19, _density_faces(), nu=0.02, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=40, kw=dict(dpdx=1e-5))
+    if name == "step_q19_les":
+        solid, sdf = backward_step(40, 16, 8, 12, 6)
+        f = channel_faces(0.06, top_bottom=BOUNCEBACK, z_periodic=True)
+        c = make_case(40, 16, 8, 19, f, nu=0.001, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=40, kw=dict(LES=1.0, spzWidth=0.25))
+    if name == "mixed_q27_cumulant":
+        c = make_case(16, 14, 12, 27, _mixed_faces(), nu=0.02)
+        return c, dict(sgs="smag", wall="ibb", collision="cumulant", steps=30, kw={})
+    if name == "cylinder_q27_cumulant_les":
+        solid, sdf = cylinder_z(28, 18, 8, 9.2, 8.7, 3.3)
+        c = make_case(28, 18, 8, 27, channel_faces(0.05), nu=0.003, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="ibb", collision="cumulant", steps=30, kw=dict(LES=1.0))
+    if name == "cavity_q27_wale":
+        c = make_case(12, 12, 12, 27, cavity_faces(0.05), nu=0.01)
+        return c, dict(sgs="wale", wall="ibb", collision="cumulant", steps=30, kw={})
+    if name == "ibm_q19":
+        c = make_case(32, 20, 6, 19, channel_faces(0.04), nu=0.02)
+        m = cylinder_markers(24, 11.3, 9.7, 2.4, 3.2)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=30, kw={}, markers=m,
+                       motion=dict(trans=(0.01, 0.0, 0.0)))
+    raise KeyError(name)
+
+
+# cases the reference itself can run (golden vectors are recorded from it)
+REFERENCE_CASES = ["cavity_q19", "cavity_q19_les", "cavity_q19_wale", "cylinder_q19_ibb_les_sponge", "cylinder_q19_bb",
+                   "cylinder2d_q19_ibb", "mixed_q19", "density_q19_dpdx", "step_q19_les", "mixed_q27_cumulant",
+                   "cylinder_q27_cumulant_les", "cavity_q27_wale", "ibm_q19"]
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| over the array."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
