@@ -105,6 +105,10 @@ def make_workload(name):
         n = 256
         c = K.make_case(n, n, n, 19, K.cavity_faces(0.05), nu=0.032)
         return c, dict(collision="rr", sgs="smag", wall="bb", les=0.0)
+    if name == "cavity128":
+        n = 128
+        c = K.make_case(n, n, n, 19, K.cavity_faces(0.05), nu=0.032)
+        return c, dict(collision="rr", sgs="smag", wall="bb", les=0.0)
     if name == "cavity256_q27":
         n = 256
         c = K.make_case(n, n, n, 27, K.cavity_faces(0.05), nu=0.032)
@@ -120,6 +124,7 @@ def make_workload(name):
 
 def describe(name, storage):
     return {"cavity256": f"lid-driven cavity D3Q19 RR {storage.upper()} 256^3, nu=0.032, lid 0.05 (synthetic)",
+            "cavity128": f"lid-driven cavity D3Q19 RR {storage.upper()} 128^3 (synthetic, profiling size)",
             "cavity256_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256^3 (synthetic)",
             "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)"}[name]
 
@@ -232,6 +237,8 @@ def main():
     ap.add_argument("--workload", default="cavity256")
     ap.add_argument("--storage", default="fp32")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="device-timed steps only (no e2e, CPU baseline or variants): the command ncu captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -273,6 +280,11 @@ def main():
     device = local if world > 1 else 0
     torch.cuda.set_device(device)
 
+    if args.profile:
+        res = run_device(args.workload, args.storage, args.steps, args.warmup, device, timing_pass=False)
+        print(json.dumps({"workload": describe(args.workload, args.storage), "ms_per_step": res["ms_per_step"],
+                          "MLUPS": res["cells"] / (res["ms_per_step"] * 1e-3) / 1e6}))
+        return 0
     with ClockSampler(device) as clk:
         res = run_device(args.workload, args.storage, args.steps, args.warmup, device)
     clocks = clk.summary()

@@ -71,7 +71,8 @@ typedef struct lbffs_desc {
 
 /* Field ids: the reference's device buffers (ns.cpp:405-436). */
 enum lbffs_field {
-    LBFFS_F = 0,         /* float32[Q*E] populations (f_d); converted to/from the storage format */
+    LBFFS_F = 0,         /* float32[Q*E] populations (f_d); converted to/from the storage format.
+                            An upload sets both population copies (f_d and fTmp_d), as initialization.hpp does. */
     LBFFS_BOUNDARY = 1,  /* int32[E] 1 on domain-face cells (boundary_d) */
     LBFFS_BOUNDARY1 = 2, /* int32[E] x-face BC code (boundary1_d), src/input.hpp:221-256 */
     LBFFS_BOUNDARY2 = 3, /* int32[E] y-face BC code */

@@ -374,10 +374,13 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
     if (fi.kind == K_F) {
         const size_t total = (size_t)c->Q * (size_t)c->E;
         const float* h = static_cast<const float*>(host);
+        // both population copies get the uploaded values: initialization.hpp fills f and fTmp alike, and
+        // cells that are never written (solid cells) must read the same values from either copy
         for (size_t s = 0; s < total; s += c->stage_elems) {
             const size_t n = (total - s < c->stage_elems) ? total - s : c->stage_elems;
             CK(cudaMemcpyAsync(c->stage, h + s, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-            CK(encode_f(c->d.storage, c->Q, c->stage, c->f[c->fcur], (long long)s, (long long)n, c->E, c->stream));
+            for (int b = 0; b < 2; b++)
+                CK(encode_f(c->d.storage, c->Q, c->stage, c->f[b], (long long)s, (long long)n, c->E, c->stream));
         }
         CK(cudaStreamSynchronize(c->stream));
         return LBFFS_OK;

@@ -31,7 +31,7 @@ build fails loudly if an anchor is missing):
 
 The host geometry code (``src/walls.hpp`` / ``src/stl.hpp``) is compiled
 by the same recipe into ``voxel_ref19`` / ``voxel_ref27`` with ``boost_stub/`` standing in for
-the one Boost call it uses.
+the one Boost call it uses, and ``src/setBoundaryConditions.hpp`` into ``case_ref``.
 
 Usage: ``python oracle/build_ref.py [--jobs N]``.  Without the reference
 checkout (e.g. on a machine the tree was copied to) it compiles the patched
@@ -172,6 +172,17 @@ def build_voxel(q, jobs_log):
     return True
 
 
+def build_case(jobs_log):
+    exe = os.path.join(OUT, "case_ref")
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-w", f"-I{os.path.join(REF, 'src')}",
+           os.path.join(HERE, "case_driver.cpp"), "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        jobs_log.append(f"case_ref: {r.stderr[-2000:]}")
+        return False
+    return True
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
@@ -201,6 +212,7 @@ def main(argv=None):
         futs = [ex.submit(build_one, *v, log) for v in variants]
         if have_ref:
             futs += [ex.submit(build_voxel, q, log) for q in (19, 27)]
+            futs.append(ex.submit(build_case, log))
         ok = all(f.result() for f in futs)
     if not ok:
         print("\n".join(log), file=sys.stderr)

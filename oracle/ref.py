@@ -113,11 +113,11 @@ class RefSolver:
                          self.nthreads)
         ibm_p = None
         if self.ibm is not None:
-            n, uT, vT, wT, rot, axis, rot_omega = self.ibm
+            n_markers, uT, vT, wT, rot, axis, rot_omega = self.ibm
             I = self._Ibm()
             for key in ("markers", "Gmx", "Gmy", "Gmz"):
                 setattr(I, key, C.cast(self._ptr(self.ibm_arrays[key]), C.POINTER(self.rt)))
-            I.n = n
+            I.n = n_markers
             I.uT, I.vT, I.wT = uT, vT, wT
             I.rotX, I.rotY, I.rotZ = rot
             I.axX, I.axY, I.axZ = axis

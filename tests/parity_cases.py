@@ -90,3 +90,26 @@ def rel_err(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def rel_l2(a, b):
+    """||a - b||_2 / ||b||_2 over the array."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+# FP32 parity bar for rho and u after N steps: relative L2 <= 1e-5 over the field (the norm the
+# storage-precision bar uses too), with a max-norm guard that catches localised mistakes.  Where
+# the reference's own FP32 run is farther than that from its FP64 run (``noise``, recorded with
+# the golden vectors: LES / WALE cases at low viscosity), the bar is twice that round-off floor.
+L2_TOL = 1e-5
+MAX_TOL = 5e-5
+
+
+def assert_fp32_parity(rho, vel, rho_ref, vel_ref, noise=0.0):
+    l2_tol = max(L2_TOL, 2.0 * noise)
+    max_tol = max(MAX_TOL, 10.0 * noise)
+    assert rel_err(rho, rho_ref) < 1e-5, ("rho", rel_err(rho, rho_ref))
+    assert rel_l2(vel, vel_ref) < l2_tol, ("u L2", rel_l2(vel, vel_ref), l2_tol)
+    assert rel_err(vel, vel_ref) < max_tol, ("u max", rel_err(vel, vel_ref), max_tol)

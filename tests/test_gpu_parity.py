@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from lbffs_gb300 import case as K
-from parity_cases import REFERENCE_CASES, build, rel_err
+from parity_cases import REFERENCE_CASES, assert_fp32_parity, build, rel_err, rel_l2
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -50,9 +50,9 @@ def test_gpu_fp32_matches_reference_golden(cuda_lib, name):
     g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
     _, _, lat = run_gpu(name)
     rho, u, v, w = lat.macros()
-    assert rel_err(rho, g["rho"]) < 1e-5
-    err = rel_err(np.stack([u, v, w]), np.stack([g["u"], g["v"], g["w"]]))
-    assert err < 1e-5, err
+    noise = float(g["noise_l2"])
+    assert_fp32_parity(rho, np.stack([u, v, w]), g["rho"], np.stack([g["u"], g["v"], g["w"]]), noise)
+    assert rel_l2(np.stack([u, v, w]), np.stack([g["u64"], g["v64"], g["w64"]])) < max(1e-5, 2.0 * noise)
     if "f" in g:
         assert rel_err(lat.download("f"), g["f"]) < 1e-5
     if "markers" in g:
@@ -65,8 +65,10 @@ def test_gpu_fp32_matches_oracle_fields(cuda_lib, oracle_built, name):
     o = run_oracle(name)
     assert rel_err(lat.download("f"), o.f) < 1e-5
     fluid = c.solid == 0
-    for fld, of in (("rho", "rho"), ("u", "u"), ("v", "v"), ("w", "w")):
-        assert rel_err(lat.download(fld)[fluid], o.field(of)[fluid]) < 1e-5, fld
+    vel = np.stack([lat.download(k)[fluid] for k in ("u", "v", "w")])
+    vel_o = np.stack([o.field(k)[fluid] for k in ("u", "v", "w")])
+    noise = float(np.load(os.path.join(GOLDEN, f"{name}.npz"))["noise_l2"])
+    assert_fp32_parity(lat.download("rho")[fluid], vel, o.field("rho")[fluid], vel_o, noise)
     tau_g, tau_o = lat.download("tau_sgs")[fluid], o.field("tauSGS")[fluid]
     assert np.abs(tau_g - tau_o).max() <= 1e-5 * max(np.abs(tau_o).max(), 1e-3)
     fw_o = np.stack([o.field("Fwx"), o.field("Fwy"), o.field("Fwz")])
@@ -242,3 +244,32 @@ def test_large_cavity_mass_and_symmetry(cuda_lib):
     w = lat.download("w").reshape(n, n, n)
     assert np.abs(u - u[::-1]).max() < 1e-5 * np.abs(u).max()
     assert np.abs(w + w[::-1]).max() < 1e-5 * max(np.abs(u).max(), 1e-6)
+
+
+@pytest.mark.parametrize("name", ["ellipsoid_q19", "ellipsoid_q27"])
+def test_reference_voxelised_body_links_and_ibb(cuda_lib, oracle_built, name):
+    """Geometry produced by the reference's own voxeliser (walls.hpp/stl.hpp): the device link table is
+    bit-exact and the interpolated bounce-back run on it matches the oracle."""
+    import lbffs_gb300 as L
+    from oracle import ref as R
+    g = np.load(os.path.join(GOLDEN, "setup_voxels.npz"))
+    q, nx, ny, nz = (int(v) for v in g[f"{name}__shape"])
+    # x / y walls as in the voxeliser run, the y-max wall moving (a lid) to drive flow past the body
+    faces = {"nxMin": K.FaceBC(K.BOUNCEBACK, 0, 0), "nxMax": K.FaceBC(K.BOUNCEBACK, 0, 0),
+             "nyMin": K.FaceBC(0, K.BOUNCEBACK, 0), "nyMax": K.FaceBC(0, K.FIXEDVELOCITY, 0, 0.05, 0, 0),
+             "nzMin": K.FaceBC(), "nzMax": K.FaceBC()}
+    c = K.make_case(nx, ny, nz, q, faces, nu=0.01, solid=g[f"{name}__solid"], sdf=g[f"{name}__sdf"])
+    assert np.array_equal(c.nei_solid, g[f"{name}__nei_solid"])
+    coll = "cumulant" if q == 27 else "rr"
+    lat = L.Lattice(nx, ny, nz, q=q, collision=coll, wall="ibb")
+    lat.load_case(c)
+    cells, masks = lat.links()
+    rc, rm = _link_table(c)
+    assert len(rc) > 500 and np.array_equal(cells, rc) and np.array_equal(masks, rm)
+    lat.step(20, les=1.0, store_fields=2)
+    lat.synchronize()
+    o = R.OracleSolver(c, sgs="smag", wall="ibb", collision=coll, real="f32")
+    o.step(20, LES=1.0)
+    assert rel_err(lat.download("f"), o.f) < 1e-5
+    fw_o = np.stack([o.field("Fwx"), o.field("Fwy"), o.field("Fwz")]).astype(np.float64).sum(1)
+    assert np.allclose(lat.force_sum(), fw_o, rtol=1e-4, atol=1e-6)

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import ref as R
-from parity_cases import REFERENCE_CASES, build, rel_err
+from parity_cases import REFERENCE_CASES, assert_fp32_parity, build, rel_err, rel_l2
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -29,10 +29,10 @@ def test_oracle_fp32_matches_reference_golden(oracle_built, name):
     g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
     _, _, o = _oracle_run(name, "f32")
     rho, u, v, w = o.macros()
-    assert rel_err(rho, g["rho"]) < 1e-6
-    vel = np.stack([u, v, w])
-    gvel = np.stack([g["u"], g["v"], g["w"]])
-    assert rel_err(vel, gvel) < 2e-5, rel_err(vel, gvel)
+    noise = float(g["noise_l2"])
+    assert_fp32_parity(rho, np.stack([u, v, w]), g["rho"], np.stack([g["u"], g["v"], g["w"]]), noise)
+    # as close to the reference's FP64 answer as the reference's FP32 run is
+    assert rel_l2(np.stack([u, v, w]), np.stack([g["u64"], g["v64"], g["w64"]])) < max(1e-5, 2.0 * noise)
 
 
 @pytest.mark.parametrize("name", REFERENCE_CASES)
