@@ -105,6 +105,123 @@ __device__ __forceinline__ void collide_rr19(float (&f)[19], float rho, const fl
     }
 }
 
+// ---- D3Q19 in moment form: all moments from the 9 opposite pairs (a = f_q + f_qbar, d = f_q - f_qbar) ----
+// The populations may be held as f_q (FP32 storage) or as deviations g_q = f_q - w_q (shifted storage,
+// DEV = true); every formula below is written in terms of r = sum_q (held value), which is rho or
+// rho - 1, so both forms share it and the large constant parts never cancel in FP32.
+struct Mom19 {
+    float r;        // sum of the held values: rho (f form) or rho - 1 (deviation form)
+    float rho;
+    float j[3];     // sum_q c_q f_q
+    float s[3][3];  // sum_q c_a c_b (held value); diagonal: sum c_a^2 f_q - 1/3 in deviation form
+};
+
+template <bool DEV>
+__device__ __forceinline__ Mom19 moments19(const float (&f)[19])
+{
+    const float a1 = f[1] + f[2], d1 = f[1] - f[2], a3 = f[3] + f[4], d3 = f[3] - f[4];
+    const float a5 = f[5] + f[6], d5 = f[5] - f[6], a7 = f[7] + f[8], d7 = f[7] - f[8];
+    const float a9 = f[9] + f[10], d9 = f[9] - f[10], a11 = f[11] + f[12], d11 = f[11] - f[12];
+    const float a13 = f[13] + f[14], d13 = f[13] - f[14], a15 = f[15] + f[16], d15 = f[15] - f[16];
+    const float a17 = f[17] + f[18], d17 = f[17] - f[18];
+    Mom19 m;
+    m.s[0][0] = (a1 + a7) + (a9 + a11) + a13;
+    m.s[1][1] = (a3 + a7) + (a9 + a15) + a17;
+    m.s[2][2] = (a5 + a11) + (a13 + a15) + a17;
+    m.r = (f[0] + a1) + (a3 + a5) + ((a7 + a9) + (a11 + a13)) + (a15 + a17);
+    m.rho = DEV ? 1.f + m.r : m.r;
+    m.j[0] = (d1 + d7) + (d9 + d11) + d13;
+    m.j[1] = (d3 + d7) - d9 + (d15 + d17);
+    m.j[2] = (d5 + d11) - d13 + (d15 - d17);
+    m.s[0][1] = m.s[1][0] = a7 - a9;
+    m.s[0][2] = m.s[2][0] = a11 - a13;
+    m.s[1][2] = m.s[2][1] = a15 - a17;
+    return m;
+}
+
+// smagorinskyTauSGS without damping, with sum_q c_a c_b feq_q = rho delta_ab / 3 + u_a u_b for the
+// reference's feq = (rho + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) w_q (fourth-order isotropy of D3Q19);
+// s_aa - r/3 is sum c_a^2 f - rho/3 in either form
+__device__ __forceinline__ float smagorinsky19(const Mom19& m, float u, float v, float w, float omega, float les,
+                                               float cs)
+{
+    const float tau = 1.f / omega;
+    const float r3 = m.r * (1.f / 3.f);
+    const float pxx = m.s[0][0] - r3 - u * u, pyy = m.s[1][1] - r3 - v * v, pzz = m.s[2][2] - r3 - w * w;
+    const float pxy = m.s[0][1] - u * v, pxz = m.s[0][2] - u * w, pyz = m.s[1][2] - v * w;
+    const float pp = pxx * pxx + pyy * pyy + pzz * pzz + 2.f * (pxy * pxy + pxz * pxz + pyz * pyz);
+    return les * 0.5f * (-tau + sqrtf(tau * tau + 18.f * 1.41421356237f * cs * cs * sqrtf(pp) / m.rho));
+}
+
+// recursive regularised collision (D3Q19 kernel.cl:3156-3309) from the moments; U without the half-force
+// shift.  Each output is written w_q * r + rho * (deviation), i.e. f_q or f_q - w_q as held.
+__device__ __forceinline__ void collide_rr19m(float (&f)[19], const Mom19& m, const float (&U)[3], float we,
+                                              float omega_b, float dpdx)
+{
+    const float third = 1.f / 3.f, k1 = 1.f - we, rho = m.rho;
+    const float ir = 1.f / rho;
+    const float r3 = m.r * third;
+    float N2[3][3], R2[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = a; b < 3; b++) {
+            const float m2 = (a == b) ? (m.s[a][a] - r3) * ir : m.s[a][b] * ir;
+            N2[a][b] = N2[b][a] = m2 - U[a] * U[b];
+            R2[a][b] = R2[b][a] = m2;
+        }
+    const float wm = (omega_b - we) * third;
+    const float nsum = N2[0][0] + N2[1][1] + N2[2][2];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        R2[a][a] -= wm * nsum + we * N2[a][a];  // omega_P on the own axis, omega_M on the others
+#pragma unroll
+        for (int b = a + 1; b < 3; b++) R2[a][b] = R2[b][a] = R2[a][b] - we * N2[a][b];
+    }
+    // T3[a][b]: c_a^2 c_b moment; Q4[a][b]: c_a^2 c_b^2 moment minus its constant 1/9
+    float T3[3][3], Q4[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            if (a == b) continue;
+            T3[a][b] = U[a] * U[a] * U[b] + k1 * (U[b] * N2[a][a] + 2.f * U[a] * N2[a][b]) + third * U[b];
+            if (b > a) {
+                const float n4 = U[b] * U[b] * N2[a][a] + U[a] * U[a] * N2[b][b] + 4.f * U[a] * U[b] * N2[a][b];
+                Q4[a][b] = Q4[b][a] = U[a] * U[a] * U[b] * U[b] + k1 * n4 + third * (R2[a][a] + R2[b][b]);
+            }
+        }
+    const float h = 0.5f * rho, qr = 0.25f * rho;
+    const float base1 = m.r * (1.f / 18.f), base2 = m.r * (1.f / 36.f);
+    const float src1 = rho * 3.f * dpdx * (1.f / 18.f), src2 = rho * 3.f * dpdx * (1.f / 36.f);
+    // axis pairs (q+, q-) = (1,2) (3,4) (5,6)
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int b = (a + 1) % 3, d = (a + 2) % 3;
+        const float A = base1 + h * (R2[a][a] - Q4[a][b] - Q4[a][d]);
+        const float B = h * (U[a] - T3[b][a] - T3[d][a]);
+        const float s = (a == 0) ? src1 : 0.f;
+        f[1 + 2 * a] = A + B + s;
+        f[2 + 2 * a] = A - B - s;
+    }
+    // diagonal planes (a,b) = (x,y) q7-10, (x,z) q11-14, (y,z) q15-18: (+,+) (-,-) (+,-) (-,+)
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+        const int a = p < 2 ? 0 : 1, b = p == 0 ? 1 : 2;
+        const float P = base2 + qr * Q4[a][b], Rr = qr * R2[a][b], X = qr * T3[a][b], Y = qr * T3[b][a];
+        const float pp = P + Rr, pm = P - Rr, xp = X + Y, xm = Y - X;
+        const float s = (a == 0) ? src2 : 0.f;
+        f[7 + 4 * p] = pp + xp + s;
+        f[8 + 4 * p] = pp - xp - s;
+        f[9 + 4 * p] = pm + xm + s;
+        f[10 + 4 * p] = pm - xm - s;
+    }
+    // rest population last: it absorbs the rounding of the other 18, so each cell's mass is kept to
+    // within one unbiased rounding (the collision conserves mass exactly in real arithmetic)
+    f[0] = m.r - (((f[1] + f[2]) + (f[3] + f[4]) + (f[5] + f[6])) +
+                  (((f[7] + f[8]) + (f[9] + f[10])) + ((f[11] + f[12]) + (f[13] + f[14]))) + ((f[15] + f[16]) + (f[17] + f[18])));
+}
+
 // 1-D backward chimera step (central moments about u -> populations at c = -1, 0, +1)
 __device__ __forceinline__ void chimera_back(float k0, float k1, float k2, float u, float& fm, float& f0, float& fp)
 {

@@ -203,7 +203,7 @@ extern "C" int lbffs_create(const lbffs_desc* desc, lbffs_ctx** out)
     if (d.wall != LBFFS_WALL_BB && d.wall != LBFFS_WALL_IBB) return fail(c, LBFFS_E_ARG, "lbffs_create: bad wall");
     if (!(d.cs > 0.f)) return fail(c, LBFFS_E_ARG, "lbffs_create: cs must be > 0");
     const long long E = (long long)d.nx * d.ny * d.nz;
-    if (E >= (1LL << 32)) return fail(c, LBFFS_E_ARG, "lbffs_create: more than 2^32 - 1 cells");
+    if (E >= (1LL << 31)) return fail(c, LBFFS_E_ARG, "lbffs_create: more than 2^31 - 1 cells");
 
     c = new lbffs_ctx();
     c->d = d;
@@ -489,6 +489,11 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
     a.sponge_mask = c->sponge_mask;
     a.sgs = c->d.sgs;
     a.wall = c->d.wall;
+    {
+        const long long sz = (c->d.nz > 1) ? (long long)c->d.nx * c->d.ny : 0;
+        for (int q = 0; q < c->Q; q++)
+            a.pull_off[q] = (int)(lat_c(c->Q, q, 0) + (long long)lat_c(c->Q, q, 1) * c->d.nx + lat_c(c->Q, q, 2) * sz);
+    }
     a.ibm_box = c->n_markers > 1 ? c->ibm_box : nullptr;
     a.err = c->d_err;
     StepConfig cfg{c->d.storage, c->d.collision, c->d.sgs, c->d.wall,
@@ -497,6 +502,10 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
     for (int s = 0; s < nsteps; s++) {
         a.f_in = c->f[c->fcur];
         a.f_out = c->f[1 - c->fcur];
+        for (int q = 0; q < c->Q; q++) {
+            a.fin_q[q] = static_cast<const char*>(a.f_in) + (size_t)q * (size_t)c->E * c->tsize;
+            a.fout_q[q] = static_cast<char*>(a.f_out) + (size_t)q * (size_t)c->E * c->tsize;
+        }
         float** mp = c->macro[c->mcur];
         float** mn = c->macro[1 - c->mcur];
         a.rho_p = mp[0];

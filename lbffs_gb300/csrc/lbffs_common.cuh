@@ -87,7 +87,10 @@ struct Codec<ST_FP32> {
     using T = float;
     static __device__ __forceinline__ float load(const T* p, float) { return __ldg(p); }
     static __device__ __forceinline__ void store(T* p, float v, float) { __stcs(p, v); }
-    static __host__ __device__ float to_float(T h, float) { return h; }
+    // held value in the bulk kernel: f itself (DEV = false)
+    static constexpr bool DEV = false;
+    static __device__ __forceinline__ float load_held(const T* p) { return __ldg(p); }
+    static __device__ __forceinline__ void store_held(T* p, float v) { __stcs(p, v); }
 };
 
 // FP16S: IEEE half of (f - w_q) * 2^15; arithmetic stays FP32.
@@ -102,6 +105,10 @@ struct Codec<ST_FP16S> {
     {
         *p = __float2half_rn((v - w) * FP16S_SCALE);
     }
+    // held value in the bulk kernel: the deviation g = f - w itself (DEV = true)
+    static constexpr bool DEV = true;
+    static __device__ __forceinline__ float load_held(const T* p) { return __half2float(__ldg(p)) * FP16S_INV; }
+    static __device__ __forceinline__ void store_held(T* p, float g) { *p = __float2half_rn(g * FP16S_SCALE); }
 };
 
 // BF16S: bfloat16 of (f - w_q); arithmetic stays FP32.
@@ -110,6 +117,9 @@ struct Codec<ST_BF16S> {
     using T = __nv_bfloat16;
     static __device__ __forceinline__ float load(const T* p, float w) { return __bfloat162float(__ldg(p)) + w; }
     static __device__ __forceinline__ void store(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
+    static constexpr bool DEV = true;
+    static __device__ __forceinline__ float load_held(const T* p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ void store_held(T* p, float g) { *p = __float2bfloat16_rn(g); }
 };
 
 // ---- kernel argument block ----
@@ -135,6 +145,11 @@ struct StepArgs {
     int sgs, wall;    // Sgs / Wall selections (runtime in the boundary kernel)
     const int* ibm_box;  // device int[6] lo/hi of the marker box (cells inside store macroscopics), or null
     int* err;            // device error word (non-finite density seen), may be null
+    // per-direction plane bases and pull offsets: population q of cell ic is read at
+    // fin_q[q][ic - pull_off[q]] and written at fout_q[q][ic]; cell indices fit in 32 bits
+    const void* fin_q[27];
+    void* fout_q[27];
+    int pull_off[27];
 };
 
 __device__ __forceinline__ bool in_box(const StepArgs& a, int i, int j, int k)

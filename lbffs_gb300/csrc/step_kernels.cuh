@@ -156,54 +156,6 @@ __device__ __forceinline__ void collide(float (&ft)[Q], float rho, float u, floa
 }
 
 // ------------------------------------------------------------------------------------------
-template <int Q, int S, int COLL, int SGS, bool LES>
-__global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
-{
-    using T = typename Codec<S>::T;
-    const int i = blockIdx.x * BULK_BX + threadIdx.x;
-    if (i >= a.nx) return;
-    const int j = blockIdx.y, k = blockIdx.z;
-    const long long ic = ((long long)k * a.ny + j) * a.nx + i;
-    const uint8_t fl = __ldg(a.flags + ic);
-    if (fl & (FL_SOLID | FL_SPECIAL)) return;
-
-    const T* fin = static_cast<const T*>(a.f_in);
-    T* fout = static_cast<T*>(a.f_out);
-    const long long sy = a.nx, sz = (a.nz > 1) ? (long long)a.nx * a.ny : 0;
-    float ft[Q];
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-        const long long off = (long long)lat_c(Q, q, 0) + (long long)lat_c(Q, q, 1) * sy + (long long)lat_c(Q, q, 2) * sz;
-        ft[q] = Codec<S>::load(fin + (long long)q * a.E + ic - off, lat_w(Q, q));
-    }
-    float rho, u, v, w;
-    macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
-    const float omega = (fl & FL_OMEGA) ? __ldg(a.omega + ic) : a.omega0;
-    float tsgs = 0.f;
-    if constexpr (SGS == SGS_WALE) {
-        const float own[3] = {u, v, w};
-        tsgs = wale_general(a, i, j, k, ic, own);
-    } else if constexpr (LES) {
-        tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
-        if (fl & FL_SDF) tsgs = damping(tsgs, __ldg(a.sdf + ic), a.cs);
-    }
-    if (a.err && !(rho == rho)) atomicOr(a.err, 1);
-    const float tau = sponge_tau(a, 1.f / omega, tsgs, i, j, k);
-    const float we = 1.f / (tau + tsgs);
-    const bool store = a.store_all || (fl & FL_STORE) || SGS == SGS_WALE || in_box(a, i, j, k);
-    if (store) {
-        a.rho_n[ic] = rho;
-        a.u_n[ic] = u;
-        a.v_n[ic] = v;
-        a.w_n[ic] = w;
-        a.tau_n[ic] = tsgs;
-    }
-    collide<Q, COLL>(ft, rho, u, v, w, we, a);
-#pragma unroll
-    for (int q = 0; q < Q; q++) Codec<S>::store(fout + (long long)q * a.E + ic, ft[q], lat_w(Q, q));
-}
-
-// ------------------------------------------------------------------------------------------
 __device__ __forceinline__ bool is_wall_code(int b) { return b == 1 || b == 4 || b == 5 || b == 6 || b == 7; }
 
 // upwindID_B with per-axis wall codes (face cells) or plain periodic wrap (other cells); -1 = missing
@@ -244,6 +196,169 @@ __device__ __forceinline__ int missing_dir(int q, const int (&b)[3])
     if (b[1] == BC_SYM) out = c1 ? lat_find(Q, c0, -c1, c2) : r;
     if (b[2] == BC_SYM) out = c2 ? lat_find(Q, c0, c1, -c2) : r;
     return out;
+}
+
+// Face-aware pull for the bulk kernel: per axis, the index correction of a periodic wrap and the
+// "missing link" flag of a wall are computed once per cell; each direction then only adds the
+// corrections of its nonzero components (the selection is resolved at compile time).
+struct FaceAxes {
+    long long wlo[3], whi[3];  // index correction when pulling across the low / high face (wrap)
+    bool mlo[3], mhi[3];       // pulling across the low / high face hits a wall (bounce-back / mirror)
+    bool sym[3];               // Symmetry code on that axis
+};
+
+__device__ __forceinline__ FaceAxes face_axes(const int (&x)[3], const int (&N)[3], const long long (&st)[3],
+                                              uint16_t bw)
+{
+    FaceAxes fa;
+    const bool face = (bw >> 9) & 1;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int b = (bw >> (3 * d)) & 7;
+        const bool wall = face && is_wall_code(b);
+        fa.wlo[d] = (x[d] == 0) ? (long long)N[d] * st[d] : 0;
+        fa.whi[d] = (x[d] == N[d] - 1) ? -(long long)N[d] * st[d] : 0;
+        fa.mlo[d] = (x[d] == 0) && wall;
+        fa.mhi[d] = (x[d] == N[d] - 1) && wall;
+        fa.sym[d] = b == BC_SYM;
+    }
+    return fa;
+}
+
+template <int Q>
+__device__ __forceinline__ int missing_dir_sym(int q, const bool (&sym)[3])
+{
+    const int c0 = lat_c(Q, q, 0), c1 = lat_c(Q, q, 1), c2 = lat_c(Q, q, 2);
+    const int r = lat_opp(Q, q);
+    if (Q == 19) {
+        if ((c0 != 0) + (c1 != 0) + (c2 != 0) < 2) return r;
+        const int fa = c0 ? lat_find(Q, -c0, c1, c2) : lat_find(Q, c0, -c1, c2);  // first nonzero axis
+        const int fb = c2 ? lat_find(Q, c0, c1, -c2) : lat_find(Q, c0, -c1, c2);  // second nonzero axis
+        const bool sa = c0 ? sym[0] : sym[1];
+        const bool sb = c2 ? sym[2] : sym[1];
+        return sa ? fa : (sb ? fb : r);
+    }
+    int out = r;
+    if (sym[0]) out = c0 ? lat_find(Q, -c0, c1, c2) : r;
+    if (sym[1]) out = c1 ? lat_find(Q, c0, -c1, c2) : r;
+    if (sym[2]) out = c2 ? lat_find(Q, c0, c1, -c2) : r;
+    return out;
+}
+
+// plane and cell that population q of cell ic is pulled from
+template <int Q>
+__device__ __forceinline__ int pull_src(int q, long long ic, const long long (&st)[3], const FaceAxes& fa, int& plane)
+{
+    long long idx = ic;
+    bool miss = false;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int c = lat_c(Q, q, d);
+        if (c == 1) {
+            idx += fa.wlo[d] - st[d];
+            miss |= fa.mlo[d];
+        } else if (c == -1) {
+            idx += fa.whi[d] + st[d];
+            miss |= fa.mhi[d];
+        }
+    }
+    plane = miss ? missing_dir_sym<Q>(q, fa.sym) : q;
+    return miss ? (int)ic : (int)idx;
+}
+
+// ------------------------------------------------------------------------------------------
+template <int Q, int S, int COLL, int SGS, bool LES>
+__global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
+{
+    using T = typename Codec<S>::T;
+    const int i = blockIdx.x * BULK_BX + threadIdx.x;
+    if (i >= a.nx) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const long long ic = ((long long)k * a.ny + j) * a.nx + i;
+    const uint8_t fl = __ldg(a.flags + ic);
+    if (fl & (FL_SOLID | FL_SPECIAL)) return;
+
+    const T* fin = static_cast<const T*>(a.f_in);
+    T* fout = static_cast<T*>(a.f_out);
+    // D3Q19 holds f (FP32 storage) or f - w (shifted storage) through the whole step; D3Q27 holds f
+    constexpr bool HELD = (Q == 19);
+    auto ld = [&](int plane, int cell, int q) {
+        const T* p = static_cast<const T*>(a.fin_q[plane]) + cell;
+        return HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+    };
+    const int ic32 = (int)ic;
+    float ft[Q];
+    if (__any_sync(__activemask(), (fl & FL_FACE) != 0)) {
+        // a warp with a domain-face cell (walls, periodic wrap, symmetry only: upwindID_B with
+        // bounce-back or mirror, kernel.cl:328-575 / 114-326); interior lanes get zero corrections
+        const long long st[3] = {1, a.nx, (a.nz > 1) ? (long long)a.nx * a.ny : 0};
+        const int x[3] = {i, j, k}, N[3] = {a.nx, a.ny, a.nz};
+        const FaceAxes fa = face_axes(x, N, st, __ldg(a.bc + ic));
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            int plane;
+            const int cell = pull_src<Q>(q, ic, st, fa, plane);
+            ft[q] = ld(plane, cell, q);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) ft[q] = ld(q, ic32 - a.pull_off[q], q);
+    }
+    const float omega = (fl & FL_OMEGA) ? __ldg(a.omega + ic) : a.omega0;
+    float rho, u, v, w, tsgs = 0.f;
+    if constexpr (Q == 19) {
+        const Mom19 m = moments19<Codec<S>::DEV>(ft);
+        rho = m.rho;
+        const float ir = 1.f / rho;
+        u = m.j[0] * ir + 0.5f * a.dpdx * ir;  // updateRhoUVW (kernel.cl:3509-3523)
+        v = m.j[1] * ir;
+        w = m.j[2] * ir;
+        if constexpr (SGS == SGS_WALE) {
+            const float own[3] = {u, v, w};
+            tsgs = wale_general(a, i, j, k, ic, own);
+        } else if constexpr (LES) {
+            tsgs = smagorinsky19(m, u, v, w, omega, a.les, a.cs);
+            if (fl & FL_SDF) tsgs = damping(tsgs, __ldg(a.sdf + ic), a.cs);
+        }
+        if (a.err && !(rho == rho)) atomicOr(a.err, 1);
+        const float tau = sponge_tau(a, 1.f / omega, tsgs, i, j, k);
+        const float we = 1.f / (tau + tsgs);
+        if (a.store_all || (fl & FL_STORE) || SGS == SGS_WALE || in_box(a, i, j, k)) {
+            a.rho_n[ic] = rho;
+            a.u_n[ic] = u;
+            a.v_n[ic] = v;
+            a.w_n[ic] = w;
+            a.tau_n[ic] = tsgs;
+        }
+        const float U[3] = {u - 0.5f * a.dpdx * ir, v, w};
+        collide_rr19m(ft, m, U, we, a.omega_b, a.dpdx);
+    } else {
+        macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
+        if constexpr (SGS == SGS_WALE) {
+            const float own[3] = {u, v, w};
+            tsgs = wale_general(a, i, j, k, ic, own);
+        } else if constexpr (LES) {
+            tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
+            if (fl & FL_SDF) tsgs = damping(tsgs, __ldg(a.sdf + ic), a.cs);
+        }
+        if (a.err && !(rho == rho)) atomicOr(a.err, 1);
+        const float tau = sponge_tau(a, 1.f / omega, tsgs, i, j, k);
+        const float we = 1.f / (tau + tsgs);
+        if (a.store_all || (fl & FL_STORE) || SGS == SGS_WALE || in_box(a, i, j, k)) {
+            a.rho_n[ic] = rho;
+            a.u_n[ic] = u;
+            a.v_n[ic] = v;
+            a.w_n[ic] = w;
+            a.tau_n[ic] = tsgs;
+        }
+        collide<Q, COLL>(ft, rho, u, v, w, we, a);
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        T* p = static_cast<T*>(a.fout_q[q]) + ic32;
+        if constexpr (HELD) Codec<S>::store_held(p, ft[q]);
+        else Codec<S>::store(p, ft[q], lat_w(Q, q));
+    }
 }
 
 template <int Q, int S, int COLL>
@@ -396,14 +511,24 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
     a.fwy[ic] = fw[1];
     a.fwz[ic] = fw[2];
 
-    float rho, u, v, w;
-    macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
-    float tsgs;
+    float rho, u, v, w, tsgs = 0.f;
+    Mom19 m19;
+    if constexpr (Q == 19) {
+        m19 = moments19<false>(ft);
+        rho = m19.rho;
+        const float ir = 1.f / rho;
+        u = m19.j[0] * ir + 0.5f * a.dpdx * ir;
+        v = m19.j[1] * ir;
+        w = m19.j[2] * ir;
+    } else {
+        macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
+    }
     if (a.sgs == SGS_WALE) {
         const float own[3] = {u, v, w};
         tsgs = wale_general(a, x[0], x[1], x[2], ic, own);
-    } else {
-        tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
+    } else if (a.les != 0.f) {
+        if constexpr (Q == 19) tsgs = smagorinsky19(m19, u, v, w, omega, a.les, a.cs);
+        else tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
         tsgs = damping(tsgs, a.sdf[ic], a.cs);
     }
     a.rho_n[ic] = rho;
@@ -413,7 +538,12 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
     a.tau_n[ic] = tsgs;
     if (a.err && !(rho == rho)) atomicOr(a.err, 1);
     const float tau = sponge_tau(a, 1.f / omega, tsgs, x[0], x[1], x[2]);
-    collide<Q, COLL>(ft, rho, u, v, w, 1.f / (tau + tsgs), a);
+    if constexpr (Q == 19) {
+        const float U[3] = {u - 0.5f * a.dpdx / rho, v, w};
+        collide_rr19m(ft, m19, U, 1.f / (tau + tsgs), a.omega_b, a.dpdx);
+    } else {
+        collide<Q, COLL>(ft, rho, u, v, w, 1.f / (tau + tsgs), a);
+    }
 #pragma unroll
     for (int q = 0; q < Q; q++) Codec<S>::store(fout + (long long)q * E + ic, ft[q], lat_w(Q, q));
 }
