@@ -169,6 +169,20 @@ int lbffs_kernel_time(lbffs_ctx* ctx, const char* name, double* total_ms, long l
 /* Counts of cells per class after the geometry commit: [fluid, special, link, store]. */
 int lbffs_cell_counts(lbffs_ctx* ctx, long long out[4]);
 
+/* No counterpart in the reference.  FP64 sum of rho over fluid cells (solid[ic] == 0) of float32
+   populations f[q*n_cells + ic] that the caller holds on `device`, written to the caller's
+   device double `out` in stream order on `stream` (0: the legacy default stream).  It is the
+   lbffs_mass reduction for callers that cannot allocate device memory when they need the check
+   (a serving loop holding a fixed HBM budget, a driver that owns its own buffers and has no
+   context): it calls no allocating routine and uses a fixed 256 KiB scratch array that every GPU
+   loading this library keeps until exit.  The first call on a device looks up that array (and may
+   load the library's device code there); make it before any stream capture.  n_cells above
+   LBFFS_NOALLOC_MAX_CELLS is rejected with LBFFS_E_ARG.  Calls share the scratch: calls whose
+   kernels overlap on the GPU race.  Errors are reported by lbffs_last_error(NULL). */
+#define LBFFS_NOALLOC_MAX_CELLS 268435456
+int lbffs_mass_noalloc(int device, const float* f, const unsigned char* solid, int q, long long n_cells,
+                       double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "lbffs_common.cuh"
 
 namespace lbffs {
@@ -40,5 +42,8 @@ cudaError_t reduce_force(const uint32_t* cells, long long n, const float* fx, co
                          double* partial, int nblocks, cudaStream_t st);
 cudaError_t reduce_mass(int storage, int Q, const void* f, const uint8_t* flags, long long E, double* partial,
                         int nblocks, cudaStream_t st);
+
+// lbffs_api.cu: record the message lbffs_last_error(NULL) returns on this thread
+void set_thread_error(const std::string& msg);
 
 }  // namespace lbffs

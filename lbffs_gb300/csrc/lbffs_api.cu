@@ -104,6 +104,8 @@ static int fail(lbffs_ctx* c, int code, const std::string& msg)
     return code;
 }
 
+void lbffs::set_thread_error(const std::string& msg) { g_thread_error = msg; }
+
 #define CK(call)                                                                                      \
     do {                                                                                              \
         cudaError_t e_ = (call);                                                                      \
