@@ -122,6 +122,123 @@ def make_workload(name):
     raise KeyError(name)
 
 
+def serving_requests(n, step_scale, seed=2024):
+    """The serving workload: Poisson arrivals (mean 200/s), each a lid-driven cavity or a channel
+    with a cylinder (50/50), grid edge log-uniform in [24, 192] cells, Re uniform in [50, 400],
+    FP32 or FP16-shifted storage (50/50), uniform in [2000, 20000] steps times step_scale."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    for _ in range(n):
+        t += rng.exponential(1.0 / 200.0)
+        out.append(dict(t=t, kind="cavity" if rng.random() < 0.5 else "channel",
+                        edge=int(round(float(np.exp(rng.uniform(np.log(24.0), np.log(192.0)))))),
+                        re=float(rng.uniform(50.0, 400.0)), storage="fp32" if rng.random() < 0.5 else "fp16s",
+                        steps=max(1, int(round(float(rng.uniform(2000, 20000)) * step_scale))),
+                        jitter=float(rng.uniform(-0.5, 0.5))))
+    return out
+
+
+def serving_case(r):
+    """Arrays of one request (populations start from rest on the device)."""
+    from lbffs_gb300 import case as K
+    from lbffs_gb300 import geometry as G
+    n = r["edge"]
+    if r["kind"] == "cavity":
+        c = K.make_case(n, n, n, 19, K.cavity_faces(0.05), nu=0.05 * n / r["re"])
+        wall = "bb"
+    else:  # 2n x n x n/4 channel, cylinder of diameter n/5 a quarter length downstream, Re on D
+        nx, ny, nz = 2 * n, n, max(4, n // 4)
+        d = n / 5.0
+        solid, sdf = G.cylinder_z(nx, ny, nz, nx / 4.0, ny / 2.0 + r["jitter"], d / 2.0)
+        c = K.make_case(nx, ny, nz, 19, K.channel_faces(0.05), nu=0.05 * d / r["re"], solid=solid, sdf=sdf)
+        wall = "ibb"
+    c.f = None
+    return c, wall
+
+
+def _serial(reqs, cases, device, per_step_sync):
+    """Each request alone on a fresh Lattice, in arrival order.  per_step_sync: one time step per
+    call followed by a synchronize, as the reference driver runs k_streamingCollision and
+    queue.finish() every step (ns.cpp:514-603); otherwise all steps in one asynchronous call."""
+    import lbffs_gb300 as L
+    t0 = time.perf_counter()
+    lat_ms, keep = [], {}
+    for k, (r, (c, wall)) in enumerate(zip(reqs, cases)):
+        wait = t0 + r["t"] - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        lat = L.Lattice(c.nx, c.ny, c.nz, storage=r["storage"], wall=wall, device=device)
+        for name in ("boundary", "boundary1", "boundary2", "boundary3", "u0", "v0", "w0", "solid", "nei_solid", "sdf",
+                     "omega"):
+            lat.upload(name, getattr(c, name))
+        lat.init_rest()
+        if per_step_sync:
+            for s in range(r["steps"]):
+                lat.step(1, store_fields=1 if s == r["steps"] - 1 else 0)
+                lat.synchronize()
+        else:
+            lat.step(r["steps"], store_fields=1)
+            lat.synchronize()
+        u = lat.download("u")
+        if k % 8 == 0:
+            keep[k] = u
+        lat.close()
+        lat_ms.append(time.perf_counter() - (t0 + r["t"]))
+    return time.perf_counter() - t0, lat_ms, keep
+
+
+def run_serving(n_req, step_scale, device, budget_gb=150.0):
+    """Served (continuous batching) vs serial plain launches of the same requests and arrivals."""
+    from lbffs_gb300.serve import Server
+    reqs = serving_requests(n_req, step_scale)
+    cases = [serving_case(r) for r in reqs]
+    cells = [c.nx * c.ny * c.nz * r["steps"] for r, (c, _) in zip(reqs, cases)]
+    bpc = [BYTES_PER_CELL[(19, r["storage"])] for r in reqs]
+
+    t_plain, lat_plain, keep = _serial(reqs, cases, device, True)
+    t_async, lat_async, _ = _serial(reqs, cases, device, False)
+
+    # served: the same arrivals, submitted from a client thread
+    srv = Server(hbm_budget=int(budget_gb * (1 << 30)), max_cases=256, steps_per_round=16, device=device)
+    ids = [None] * n_req
+    t0 = time.perf_counter()
+
+    def client():
+        for k, (r, (c, wall)) in enumerate(zip(reqs, cases)):
+            wait = t0 + r["t"] - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            ids[k] = srv.submit(c, r["steps"], storage=r["storage"], wall=wall, from_rest=True)
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    for cid in ids:
+        srv.wait(cid, 3600.0)
+    t_served = time.perf_counter() - t0
+    st = srv.stats()
+    same = all(np.array_equal(srv.result(ids[k], "u"), u) for k, u in keep.items())
+    srv.close()
+    peak, _ = peaks()
+    tot = float(sum(cells))
+    bytes_tot = float(sum(cl * b for cl, b in zip(cells, bpc)))
+    return {"requests": n_req, "step_scale": step_scale,
+            "sample": f"{n_req} requests of the serving workload (seed 2024), steps scaled by {step_scale}",
+            "solves_per_s": n_req / t_served, "serial_solves_per_s": n_req / t_plain,
+            "speedup_vs_serial": t_plain / t_served,
+            "serial_async_solves_per_s": n_req / t_async, "speedup_vs_serial_async": t_async / t_served,
+            "latency_p50_s": st["latency_p50_s"], "latency_p99_s": st["latency_p99_s"],
+            "queue_wait_p99_s": st["queue_wait_p99_s"],
+            "serial_latency_p50_s": float(np.percentile(lat_plain, 50)),
+            "serial_latency_p99_s": float(np.percentile(lat_plain, 99)),
+            "MLUPS": tot / t_served / 1e6, "serial_MLUPS": tot / t_plain / 1e6,
+            "hbm_frac": bytes_tot / t_served / 1e9 / peak,
+            "hbm_peak_GB": st["hbm_peak"] / 1e9, "rounds": st["rounds"], "graph_builds": st["graph_builds"],
+            "identical_to_serial": bool(same), "compared": len(keep),
+            "serial": "one Lattice per request in arrival order, one step per call + synchronize "
+                      "(the reference driver's launch + queue.finish per step)"}
+
+
 def describe(name, storage):
     return {"cavity256": f"lid-driven cavity D3Q19 RR {storage.upper()} 256^3, nu=0.032, lid 0.05 (synthetic)",
             "cavity128": f"lid-driven cavity D3Q19 RR {storage.upper()} 128^3 (synthetic, profiling size)",
@@ -153,15 +270,18 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
     ms = e0.elapsed_time(e1)
     counts = lat.cell_counts()
     out = {"ms_per_step": ms / steps, "cells": c.elements, "fluid": counts["fluid"], "special": counts["special"],
-           "launches_per_step": 2 if counts["special"] > 0 else 1, "lat": lat, "case": c, "sel": sel}
+           # k_halo (ghost layer) + k_bulk every step, k_special when the case has special cells
+           "launches_per_step": 3 if counts["special"] > 0 else 2, "lat": lat, "case": c, "sel": sel}
     if timing_pass:
         lat.set_timing(True)
         lat.step(steps, les=sel["les"], store_fields=0)
         bulk_ms, n = lat.kernel_time("bulk")
         sp_ms, nsp = lat.kernel_time("special")
+        h_ms, nh = lat.kernel_time("halo")
         lat.set_timing(False)
         out["bulk_ms"] = bulk_ms / max(n, 1)
         out["special_ms"] = sp_ms / max(nsp, 1)
+        out["halo_ms"] = h_ms / max(nh, 1)
     return out
 
 
@@ -237,6 +357,9 @@ def main():
     ap.add_argument("--workload", default="cavity256")
     ap.add_argument("--storage", default="fp32")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--requests", type=int, default=512, help="serving workload: number of requests")
+    ap.add_argument("--step-scale", type=float, default=1.0, help="serving workload: step count scale")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="device-timed steps only (no e2e, CPU baseline or variants): the command ncu captures")
     args = ap.parse_args()
@@ -280,6 +403,13 @@ def main():
     device = local if world > 1 else 0
     torch.cuda.set_device(device)
 
+    if args.workload == "serving":
+        if rank == 0:
+            out = run_serving(args.requests, args.step_scale, device)
+            out.update({"metric": "served solves/s", "unit": "solves/s", "value": out["solves_per_s"],
+                        "higher_is_better": True, "n_gpus": 1, "dtype": "f32/fp16s", "data": "synthetic"})
+            print(json.dumps(out))
+        return 0
     if args.profile:
         res = run_device(args.workload, args.storage, args.steps, args.warmup, device, timing_pass=False)
         print(json.dumps({"workload": describe(args.workload, args.storage), "ms_per_step": res["ms_per_step"],
@@ -319,6 +449,7 @@ def main():
                 variants[f"{vname}_{vst}"] = {
                     "workload": describe(vname, vst), "MLUPS": r["cells"] / (r["ms_per_step"] * 1e-3) / 1e6,
                     "ms_per_step": r["ms_per_step"], "bulk_ms": r["bulk_ms"], "special_ms": r["special_ms"],
+                    "halo_ms": r["halo_ms"],
                     "bulk_GBps": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9,
                     "bulk_frac_of_peak": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9 / peak,
                     "bytes_per_cell": vb}
@@ -326,6 +457,13 @@ def main():
                 del r
             except Exception as ex:  # a failing variant must not hide the headline
                 variants[f"{vname}_{vst}"] = {"error": str(ex)[:200]}
+
+    serving = None
+    if rank == 0 and not args.no_serving and args.workload == "cavity256":
+        try:
+            serving = run_serving(48, 0.1, device)
+        except Exception as ex:  # the serving sample must not hide the headline
+            serving = {"error": str(ex)[:300]}
 
     cpu = None
     if rank == 0:
@@ -349,11 +487,14 @@ def main():
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "kernel": "k_bulk", "bytes_per_cell": bpc, "cells_per_launch": n_bulk,
-                         "launch_ms": res["bulk_ms"], "peak_source": f"{peak_kind} hbm_gbs"},
+                         "launch_ms": res["bulk_ms"], "peak_source": f"{peak_kind} hbm_gbs",
+                         "step_kernels_ms": {"k_bulk": res["bulk_ms"], "k_special": res["special_ms"],
+                                             "k_halo": res["halo_ms"]}},
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": res["launches_per_step"] * args.steps,
             "variants": variants,
+            "serving": serving,
         }
         print(json.dumps(line))
     if world > 1:

@@ -169,6 +169,71 @@ int lbffs_kernel_time(lbffs_ctx* ctx, const char* name, double* total_ms, long l
 /* Counts of cells per class after the geometry commit: [fluid, special, link, store]. */
 int lbffs_cell_counts(lbffs_ctx* ctx, long long out[4]);
 
+/* Set both population copies to the rest equilibrium rho = 1, u = 0 (f_q = w_q), the state
+   initialization.hpp writes for a fluid at rest, without a host upload of F. */
+int lbffs_init_rest(lbffs_ctx* ctx);
+
+/* ---- Serving: many solves resident on one GPU, advanced together ----
+   The reference runs one case per process (ns.cpp); this server keeps many cases resident and
+   advances all of them with one batched launch per kernel per step (CUDA graph replay), admitting
+   queued cases as device memory and slots free up.  Each case is described exactly like a
+   context (lbffs_desc + the reference's arrays) and computes the same numbers as lbffs_step.
+   Supported: q = 19, RR collision, Smagorinsky SGS (LES on or off), BB or IBB walls, any storage;
+   no IBM markers. */
+typedef struct lbffs_server lbffs_server;
+
+typedef struct lbffs_server_desc {
+    int device;            /* CUDA device ordinal */
+    size_t hbm_budget;     /* bytes of device memory the resident cases may hold */
+    int max_cases;         /* resident cases at once */
+    int steps_per_round;   /* steps per graph replay between admission / retirement checks */
+} lbffs_server_desc;
+
+/* One solve.  Array pointers are read during lbffs_server_submit only (copied).  boundary..
+   boundary3 and solid / nei_solid are required; sdf, u0, v0, w0, omega may be NULL (10000, 0, 1);
+   f NULL starts from rest (lbffs_init_rest). */
+typedef struct lbffs_case {
+    lbffs_desc desc;
+    lbffs_step_params params;   /* store_fields is ignored: results hold the final step's fields */
+    long long nsteps;
+    int want_f;                 /* also keep the final populations */
+    const int *boundary, *boundary1, *boundary2, *boundary3;
+    const unsigned char *solid, *nei_solid;
+    const float *sdf, *u0, *v0, *w0, *omega;
+    const float* f;
+} lbffs_case;
+
+enum lbffs_case_state { LBFFS_CASE_QUEUED = 0, LBFFS_CASE_RUNNING = 1, LBFFS_CASE_DONE = 2, LBFFS_CASE_FAILED = -1 };
+
+typedef struct lbffs_server_stats {
+    long long submitted, completed, failed, resident, queued;
+    long long rounds, graph_builds;
+    double cell_updates;                        /* lattice updates of completed cases */
+    double elapsed_s;                           /* first submission to last completion */
+    double latency_p50_s, latency_p99_s, latency_mean_s, latency_max_s;  /* submit to result */
+    double queue_wait_p50_s, queue_wait_p99_s;  /* submit to admission */
+    size_t hbm_in_use, hbm_peak, hbm_capacity;
+} lbffs_server_stats;
+
+int lbffs_server_create(const lbffs_server_desc* desc, lbffs_server** out);
+/* Stops the loop (cases still queued or running are abandoned) and frees everything. */
+int lbffs_server_destroy(lbffs_server* srv);
+/* Queue a solve; *id identifies it in the calls below.  LBFFS_E_UNSUPPORTED for a case outside the
+   supported set, LBFFS_E_ARG when it can never fit the budget. */
+int lbffs_server_submit(lbffs_server* srv, const lbffs_case* c, long long* id);
+/* Current state (enum lbffs_case_state). */
+int lbffs_server_poll(lbffs_server* srv, long long id, int* state);
+/* Block until the case is done or failed, or timeout_s passes (LBFFS_E_STATE on timeout). */
+int lbffs_server_wait(lbffs_server* srv, long long id, double timeout_s);
+/* Copy a result field of a finished case: LBFFS_RHO, LBFFS_U, LBFFS_V, LBFFS_W (float32[E]) or
+   LBFFS_F (float32[Q*E], when want_f was set). */
+int lbffs_server_result(lbffs_server* srv, long long id, int field, void* host, size_t bytes);
+/* Drop a finished case's results. */
+int lbffs_server_release(lbffs_server* srv, long long id);
+int lbffs_server_get_stats(lbffs_server* srv, lbffs_server_stats* out);
+/* Message of the last failure of case id (or of the server when id < 0). */
+const char* lbffs_server_error(lbffs_server* srv, long long id);
+
 /* No counterpart in the reference.  FP64 sum of rho over fluid cells (solid[ic] == 0) of float32
    populations f[q*n_cells + ic] that the caller holds on `device`, written to the caller's
    device double `out` in stream order on `stream` (0: the legacy default stream).  It is the

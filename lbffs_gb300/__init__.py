@@ -91,6 +91,7 @@ def load_library():
         "lbffs_set_timing": ([vp, i], i),
         "lbffs_kernel_time": ([vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)], i),
         "lbffs_cell_counts": ([vp, C.POINTER(C.c_longlong)], i),
+        "lbffs_init_rest": ([vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -169,6 +170,10 @@ class Lattice:
     def step(self, n=1, dpdx=0.0, les=0.0, omega_b=0.1, spz_width=0.1, clim=0.01, rho_av=1.0, store_fields=1):
         p = StepParams(dpdx, rho_av, les, omega_b, spz_width, clim, int(store_fields))
         self._check(self.lib.lbffs_step(self.h, C.byref(p), int(n)))
+
+    def init_rest(self):
+        """Both population copies at rest (f_q = w_q) without a host upload."""
+        self._check(self.lib.lbffs_init_rest(self.h))
 
     def synchronize(self):
         self._check(self.lib.lbffs_synchronize(self.h))

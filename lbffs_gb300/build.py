@@ -1,7 +1,7 @@
 """Build recipe for ``lbffs_gb300/liblbffs_cuda.so`` (the C-ABI CUDA library).
 
-Compiles every ``csrc/*.cu`` translation unit for sm_103a in parallel with nvcc and
-links them into one shared library next to this file.  Rebuilds only what changed.
+Compiles every ``csrc/*.cu`` / ``*.cpp`` translation unit for sm_103a in parallel with nvcc
+and links them into one shared library next to this file.  Rebuilds only what changed.
 """
 from __future__ import annotations
 
@@ -46,14 +46,19 @@ def build(verbose=False, extra_flags=None, jobs=None):
     hdrs = _headers()
     units = []  # (source, object, defines)
     for f in sorted(os.listdir(CSRC)):
-        if f.endswith(".cu") and f != "step_inst.cu":
-            units.append((f, f[:-3] + ".o", []))
-    # the step kernels: one object per (lattice, storage, bulk/special) so they compile in parallel
-    for q in (19, 27):
+        if f.endswith((".cu", ".cpp")) and f not in ("step_inst.cu", "batch_inst.cu"):
+            units.append((f, os.path.splitext(f)[0] + ".o", []))
+    # batched kernels of the server: one object per storage format
+    for st in (0, 1, 2):
+        units.append(("batch_inst.cu", f"batch_s{st}.o", [f"-DLBFFS_S={st}"]))
+    # the step kernels: one object per (lattice, storage, collision, kernel variant) so they compile
+    # in parallel (step_inst.cu lists the parts)
+    for q, colls in ((19, (0,)), (27, (0, 1))):
         for st in (0, 1, 2):
-            for part, name in ((0, "bulk"), (1, "special")):
-                units.append(("step_inst.cu", f"step_q{q}_s{st}_{name}.o",
-                              [f"-DLBFFS_Q={q}", f"-DLBFFS_S={st}", f"-DLBFFS_PART={part}"]))
+            for coll in colls:
+                for part in (0, 1, 2, 3):
+                    units.append(("step_inst.cu", f"step_q{q}_s{st}_c{coll}_p{part}.o",
+                                  [f"-DLBFFS_Q={q}", f"-DLBFFS_S={st}", f"-DLBFFS_C={coll}", f"-DLBFFS_PART={part}"]))
     cmds = []
     objs = []
     for s, o, defs in units:
@@ -63,7 +68,7 @@ def build(verbose=False, extra_flags=None, jobs=None):
         if _stale(obj, [src] + hdrs):
             cmds.append([nvcc(), *ARCH, *NVCC_FLAGS, *defs, *(extra_flags or []), "-c", src, "-o", obj])
     # longest compiles first
-    cmds.sort(key=lambda c: ("step_q27" not in c[-1], "special" not in c[-1]))
+    cmds.sort(key=lambda c: ("_c1_" not in c[-1], "step_q27" not in c[-1]))
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -76,7 +81,7 @@ def build(verbose=False, extra_flags=None, jobs=None):
             if verbose and (r.stdout or r.stderr):
                 print(r.stdout + r.stderr)
     if cmds or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)

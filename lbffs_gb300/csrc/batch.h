@@ -1,0 +1,42 @@
+// Batched step kernels of the server: one launch advances every resident case of a group
+// (same storage format and LES switch).  A case is described by the kernel arguments of its two
+// ping-pong parities; its device step counter picks the parity and stops it at exactly nsteps.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "launch.h"
+
+namespace lbffs {
+
+struct BatchCase {
+    StepArgs args[2];  // args[p]: source populations and macroscopics are copy p
+    long long nsteps;  // steps the case runs in total
+    int slot;          // index of the case's step counter
+    int tiles_x;       // bulk tiles per row: ceil(nx / (BULK_BX * BULK_V))
+};
+
+// Bulk step of every case in cases[0..ncases): CTA b runs tile b - tile_start[c] of the case c
+// with tile_start[c] <= b < tile_start[c + 1] (ntiles = tile_start[ncases]).
+cudaError_t batch_bulk(int storage, bool les, const BatchCase* cases, const int* tile_start, int ncases, int ntiles,
+                       const long long* done, cudaStream_t st);
+// Boundary step: thread t runs entry t - sp_start[c] of case c's special list.
+cudaError_t batch_special(int storage, const BatchCase* cases, const long long* sp_start, int ncases,
+                          long long nspecial, const long long* done, cudaStream_t st);
+// Ghost layers: thread t fills ghost thread t - h_start[c] of case c's source populations.
+cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nthreads,
+                       const long long* done, cudaStream_t st);
+// Advance the step counters of the listed slots that have not reached their nsteps.
+cudaError_t batch_tick(const int* slots, const long long* nsteps, int n, long long* done, cudaStream_t st);
+
+// per storage format (batch_inst.cu compiled once per format)
+cudaError_t batch_bulk_s0(bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s1(bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s2(bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
+cudaError_t batch_special_s0(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_halo_s0(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_halo_s1(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_halo_s2(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_special_s1(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_special_s2(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+
+}  // namespace lbffs

@@ -1,0 +1,119 @@
+// Batched D3Q19 step kernels for one storage format (compiled once per LBFFS_S).  They run the
+// same per-tile and per-cell code as k_bulk / k_special (bulk_block, special_cell), so a case
+// computes the same numbers alone, in a batch, or through lbffs_step.
+#include <type_traits>
+
+#include "batch.h"
+#include "step_kernels.cuh"
+
+#ifndef LBFFS_S
+#error "compile with -DLBFFS_S=<storage>"
+#endif
+
+namespace lbffs {
+namespace {
+
+constexpr int S = LBFFS_S;
+
+// last index c in [0, n) with start[c] <= key (start ascending, start[0] = 0)
+template <class T>
+__device__ __forceinline__ int find_case(const T* __restrict__ start, int n, T key)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(start + mid) <= key) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool LES>
+__global__ void __launch_bounds__(BULK_BX) k_bulk_batch(const BatchCase* __restrict__ cases,
+                                                        const int* __restrict__ tile_start, int ncases,
+                                                        const long long* __restrict__ done)
+{
+    __shared__ StepArgs sa;
+    __shared__ int s_case, s_parity, s_last;
+    if (threadIdx.x == 0) {
+        const int c = find_case<int>(tile_start, ncases, (int)blockIdx.x);
+        const long long d = done[cases[c].slot];
+        s_case = c;
+        s_parity = d < cases[c].nsteps ? (int)(d & 1) : -1;
+        s_last = d + 1 == cases[c].nsteps;
+    }
+    __syncthreads();
+    if (s_parity < 0) return;  // the case has finished; it leaves the batch at the next rebuild
+    const int* src = reinterpret_cast<const int*>(&cases[s_case].args[s_parity]);
+    int* dst = reinterpret_cast<int*>(&sa);
+    for (int w = threadIdx.x; w < (int)(sizeof(StepArgs) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+    if (threadIdx.x == 0 && s_last) sa.store_all = 1;  // full macroscopic fields on the final step
+    __syncthreads();
+    const int tile = (int)blockIdx.x - tile_start[s_case];
+    const int tx = cases[s_case].tiles_x;
+    const int xb = tile % tx, row = tile / tx;
+    bulk_block<19, S, COLL_RR, SGS_SMAG, LES>(sa, xb, row % sa.ny, row / sa.ny);
+}
+
+__global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* __restrict__ cases,
+                                                              const long long* __restrict__ sp_start, int ncases,
+                                                              const long long* __restrict__ done)
+{
+    const long long t = (long long)blockIdx.x * SPECIAL_BS + threadIdx.x;
+    if (t >= sp_start[ncases]) return;
+    const int c = find_case<long long>(sp_start, ncases, t);
+    const long long d = done[cases[c].slot];
+    if (d >= cases[c].nsteps) return;
+    special_cell<19, S, COLL_RR>(cases[c].args[d & 1], t - sp_start[c]);
+}
+
+using W = typename std::conditional<S == ST_FP32, uint32_t, uint16_t>::type;
+
+__global__ void __launch_bounds__(128) k_halo_batch(const BatchCase* __restrict__ cases,
+                                                    const long long* __restrict__ h_start, int ncases,
+                                                    const long long* __restrict__ done)
+{
+    const long long t = (long long)blockIdx.x * 128 + threadIdx.x;
+    if (t >= h_start[ncases]) return;
+    const int c = find_case<long long>(h_start, ncases, t);
+    const long long d = done[cases[c].slot];
+    if (d >= cases[c].nsteps) return;
+    const StepArgs& a = cases[c].args[d & 1];
+    const PadGeom g{a.nx, a.ny, a.nz, a.px, a.pxy, a.porg, a.pE};
+    // the ghosts of this step's source copy (k_bulk / k_special read it only after this launch)
+    halo_thread<19, W>(static_cast<W*>(const_cast<void*>(a.f_in)), a.flags, a.bc, g, t - h_start[c]);
+}
+
+}  // namespace
+
+#define LBFFS_CAT2(a, b) a##b
+#define LBFFS_CAT(a, b) LBFFS_CAT2(a, b)
+
+cudaError_t LBFFS_CAT(batch_bulk_s, LBFFS_S)(bool les, const BatchCase* cases, const int* tile_start, int ncases,
+                                             int ntiles, const long long* done, cudaStream_t st)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    if (les) k_bulk_batch<true><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+    else k_bulk_batch<false><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+    return cudaGetLastError();
+}
+
+cudaError_t LBFFS_CAT(batch_special_s, LBFFS_S)(const BatchCase* cases, const long long* sp_start, int ncases,
+                                                long long nspecial, const long long* done, cudaStream_t st)
+{
+    if (nspecial <= 0) return cudaSuccess;
+    const unsigned nb = (unsigned)((nspecial + SPECIAL_BS - 1) / SPECIAL_BS);
+    k_special_batch<<<nb, SPECIAL_BS, 0, st>>>(cases, sp_start, ncases, done);
+    return cudaGetLastError();
+}
+
+cudaError_t LBFFS_CAT(batch_halo_s, LBFFS_S)(const BatchCase* cases, const long long* h_start, int ncases,
+                                             long long nthreads, const long long* done, cudaStream_t st)
+{
+    if (nthreads <= 0) return cudaSuccess;
+    k_halo_batch<<<(unsigned)((nthreads + 127) / 128), 128, 0, st>>>(cases, h_start, ncases, done);
+    return cudaGetLastError();
+}
+
+}  // namespace lbffs

@@ -109,6 +109,8 @@ __device__ __forceinline__ void collide_rr19(float (&f)[19], float rho, const fl
 // The populations may be held as f_q (FP32 storage) or as deviations g_q = f_q - w_q (shifted storage,
 // DEV = true); every formula below is written in terms of r = sum_q (held value), which is rho or
 // rho - 1, so both forms share it and the large constant parts never cancel in FP32.
+// Moments of the held values.  With a held scale HS (2^15 for FP16S storage) r, j and s are HS
+// times the moments of f (f form) or of f - w (deviation form); rho is unscaled.
 struct Mom19 {
     float r;        // sum of the held values: rho (f form) or rho - 1 (deviation form)
     float rho;
@@ -116,7 +118,7 @@ struct Mom19 {
     float s[3][3];  // sum_q c_a c_b (held value); diagonal: sum c_a^2 f_q - 1/3 in deviation form
 };
 
-template <bool DEV>
+template <bool DEV, int HS = 1>
 __device__ __forceinline__ Mom19 moments19(const float (&f)[19])
 {
     const float a1 = f[1] + f[2], d1 = f[1] - f[2], a3 = f[3] + f[4], d3 = f[3] - f[4];
@@ -129,7 +131,8 @@ __device__ __forceinline__ Mom19 moments19(const float (&f)[19])
     m.s[1][1] = (a3 + a7) + (a9 + a15) + a17;
     m.s[2][2] = (a5 + a11) + (a13 + a15) + a17;
     m.r = (f[0] + a1) + (a3 + a5) + ((a7 + a9) + (a11 + a13)) + (a15 + a17);
-    m.rho = DEV ? 1.f + m.r : m.r;
+    if constexpr (HS == 1) m.rho = DEV ? 1.f + m.r : m.r;
+    else m.rho = DEV ? 1.f + m.r * (1.f / HS) : m.r * (1.f / HS);
     m.j[0] = (d1 + d7) + (d9 + d11) + d13;
     m.j[1] = (d3 + d7) - d9 + (d15 + d17);
     m.j[2] = (d5 + d11) - d13 + (d15 - d17);
@@ -142,24 +145,34 @@ __device__ __forceinline__ Mom19 moments19(const float (&f)[19])
 // smagorinskyTauSGS without damping, with sum_q c_a c_b feq_q = rho delta_ab / 3 + u_a u_b for the
 // reference's feq = (rho + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) w_q (fourth-order isotropy of D3Q19);
 // s_aa - r/3 is sum c_a^2 f - rho/3 in either form
+template <int HS = 1>
 __device__ __forceinline__ float smagorinsky19(const Mom19& m, float u, float v, float w, float omega, float les,
                                                float cs)
 {
     const float tau = 1.f / omega;
     const float r3 = m.r * (1.f / 3.f);
-    const float pxx = m.s[0][0] - r3 - u * u, pyy = m.s[1][1] - r3 - v * v, pzz = m.s[2][2] - r3 - w * w;
-    const float pxy = m.s[0][1] - u * v, pxz = m.s[0][2] - u * w, pyz = m.s[1][2] - v * w;
+    float pxx, pyy, pzz, pxy, pxz, pyz;
+    if constexpr (HS == 1) {
+        pxx = m.s[0][0] - r3 - u * u, pyy = m.s[1][1] - r3 - v * v, pzz = m.s[2][2] - r3 - w * w;
+        pxy = m.s[0][1] - u * v, pxz = m.s[0][2] - u * w, pyz = m.s[1][2] - v * w;
+    } else {
+        constexpr float is = 1.f / HS;
+        pxx = (m.s[0][0] - r3) * is - u * u, pyy = (m.s[1][1] - r3) * is - v * v, pzz = (m.s[2][2] - r3) * is - w * w;
+        pxy = m.s[0][1] * is - u * v, pxz = m.s[0][2] * is - u * w, pyz = m.s[1][2] * is - v * w;
+    }
     const float pp = pxx * pxx + pyy * pyy + pzz * pzz + 2.f * (pxy * pxy + pxz * pxz + pyz * pyz);
     return les * 0.5f * (-tau + sqrtf(tau * tau + 18.f * 1.41421356237f * cs * cs * sqrtf(pp) / m.rho));
 }
 
 // recursive regularised collision (D3Q19 kernel.cl:3156-3309) from the moments; U without the half-force
-// shift.  Each output is written w_q * r + rho * (deviation), i.e. f_q or f_q - w_q as held.
+// shift.  Each output is written w_q * r + rho * (deviation), i.e. f_q or f_q - w_q as held, times the
+// held scale HS (a power of two, so the scaled results are the unscaled ones times HS exactly).
+template <int HS = 1>
 __device__ __forceinline__ void collide_rr19m(float (&f)[19], const Mom19& m, const float (&U)[3], float we,
                                               float omega_b, float dpdx)
 {
     const float third = 1.f / 3.f, k1 = 1.f - we, rho = m.rho;
-    const float ir = 1.f / rho;
+    const float ir = (1.f / rho) * (1.f / HS);
     const float r3 = m.r * third;
     float N2[3][3], R2[3][3];
 #pragma unroll
@@ -191,9 +204,9 @@ __device__ __forceinline__ void collide_rr19m(float (&f)[19], const Mom19& m, co
                 Q4[a][b] = Q4[b][a] = U[a] * U[a] * U[b] * U[b] + k1 * n4 + third * (R2[a][a] + R2[b][b]);
             }
         }
-    const float h = 0.5f * rho, qr = 0.25f * rho;
+    const float h = rho * (0.5f * HS), qr = rho * (0.25f * HS);
     const float base1 = m.r * (1.f / 18.f), base2 = m.r * (1.f / 36.f);
-    const float src1 = rho * 3.f * dpdx * (1.f / 18.f), src2 = rho * 3.f * dpdx * (1.f / 36.f);
+    const float src1 = rho * 3.f * dpdx * (1.f / 18.f) * HS, src2 = rho * 3.f * dpdx * (1.f / 36.f) * HS;
     // axis pairs (q+, q-) = (1,2) (3,4) (5,6)
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -341,19 +354,8 @@ __device__ __forceinline__ void collide_cumulant(float (&f)[27], float rho, floa
     const float C110 = K[1][1][0], C101 = K[1][0][1], C011 = K[0][1][1];
     const float C210 = K[2][1][0], C201 = K[2][0][1], C021 = K[0][2][1], C120 = K[1][2][0], C102 = K[1][0][2],
                 C012 = K[0][1][2], C111 = K[1][1][1];
-    const float C211 = K[2][1][1] - (K[2][0][0] * K[0][1][1] + 2.f * K[1][1][0] * K[1][0][1]) * ir;
-    const float C121 = K[1][2][1] - (K[0][2][0] * K[1][0][1] + 2.f * K[1][1][0] * K[0][1][1]) * ir;
-    const float C112 = K[1][1][2] - (K[0][0][2] * K[1][1][0] + 2.f * K[1][0][1] * K[0][1][1]) * ir;
-    const float C220 = K[2][2][0] - (K[2][0][0] * K[0][2][0] + 2.f * K[1][1][0] * K[1][1][0]) * ir;
-    const float C202 = K[2][0][2] - (K[0][0][2] * K[2][0][0] + 2.f * K[1][0][1] * K[1][0][1]) * ir;
-    const float C022 = K[0][2][2] - (K[0][2][0] * K[0][0][2] + 2.f * K[0][1][1] * K[0][1][1]) * ir;
-    const float C122 = K[1][2][2] - (K[0][0][2] * K[1][2][0] + K[0][2][0] * K[1][0][2] + 4.f * K[0][1][1] * K[1][1][1] +
-                                     2.f * (K[1][0][1] * K[0][2][1] + K[1][1][0] * K[0][1][2])) * ir;
-    const float C212 = K[2][1][2] - (K[2][0][0] * K[0][1][2] + K[0][0][2] * K[2][1][0] + 4.f * K[1][0][1] * K[1][1][1] +
-                                     2.f * (K[1][1][0] * K[1][0][2] + K[0][1][1] * K[2][0][1])) * ir;
-    const float C221 = K[2][2][1] - (K[0][2][0] * K[2][0][1] + K[2][0][0] * K[0][2][1] + 4.f * K[1][1][0] * K[1][1][1] +
-                                     2.f * (K[0][1][1] * K[2][1][0] + K[1][0][1] * K[1][2][0])) * ir;
-    // C222 relaxes to 0 (omega10 = 1, kernel.cl:2478), so it is not formed.
+    // the fourth-order cumulants C211..C022, the fifth-order C122..C221 and C222 relax to their
+    // equilibrium with rate 1 (omega6..omega10 = 1, D3Q27 kernel.cl:2474-2478), so they are not formed
 
     const float w1 = we, w2 = omega_b;
     const float w3 = 8.f * (w1 - 2.f) * (w2 * (3.f * w1 - 1.f) - 5.f * w1) /

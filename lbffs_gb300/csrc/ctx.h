@@ -1,0 +1,95 @@
+// The context behind the C ABI (include/lbffs_cuda.h), shared by the single-lattice entry points
+// and the server: device buffers of one lattice, its geometry lists and its step state.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lbffs_cuda.h"
+#include "arena.h"
+#include "ibm.h"
+#include "launch.h"
+
+struct lbffs_ctx {
+    lbffs_desc d{};
+    int Q = 19;
+    long long E = 0;
+    size_t tsize = 4;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    std::string err = "no error";
+
+    void* f[2] = {nullptr, nullptr};
+    int fcur = 0;
+    int* iarr[4] = {nullptr, nullptr, nullptr, nullptr};  // boundary, boundary1..3 as uploaded
+    uint8_t *solid = nullptr, *nei = nullptr, *flags = nullptr;
+    uint16_t* bc = nullptr;
+    float *u0 = nullptr, *v0 = nullptr, *w0 = nullptr, *omega = nullptr, *sdf = nullptr;
+    float* macro[2][5] = {{nullptr}};
+    int mcur = 0;
+    float* fw[3] = {nullptr, nullptr, nullptr};
+    float* g[3] = {nullptr, nullptr, nullptr};
+    uint32_t* special = nullptr;
+    long long n_special = 0;
+    lbffs::PadGeom pg{};
+    long long counts[4] = {0, 0, 0, 0};
+    float omega0 = 1.f;
+    int sponge_mask = 0;
+    bool dirty = true;
+    int* d_err = nullptr;
+    float* stage = nullptr;
+    size_t stage_elems = 0;
+    double* partial = nullptr;
+    int partial_blocks = 0;
+
+    // IBM
+    int n_markers = 0;
+    float* markers = nullptr;
+    float* gm = nullptr;
+    double* ibm_acc = nullptr;
+    double* ibm_lag = nullptr;
+    int* ibm_box = nullptr;
+    long long* ibm_t = nullptr;
+    lbffs::IbmMotion motion{};
+
+    // server cases: device memory from the server's arena, the server's stream and staging
+    lbffs::Arena* arena = nullptr;
+    bool own_stream = true, own_stage = true;
+
+    // timing
+    bool timing = false;
+    struct Ev {
+        cudaEvent_t a, b;
+        int kind;
+    };
+    std::vector<Ev> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[4] = {0, 0, 0, 0};
+    long long launches[4] = {0, 0, 0, 0};
+};
+
+namespace lbffs {
+
+// record msg as the context's (and this thread's) last error and return code
+int ctx_fail(lbffs_ctx* c, int code, const std::string& msg);
+// zero-filled device allocation from the context's arena (server cases) or cudaMalloc
+cudaError_t ctx_alloc_bytes(lbffs_ctx* c, void** p, size_t bytes);
+template <class T>
+inline cudaError_t ctx_alloc(lbffs_ctx* c, T** p, size_t n)
+{
+    return ctx_alloc_bytes(c, reinterpret_cast<void**>(p), n * sizeof(T) + 16);
+}
+void ctx_free(lbffs_ctx* c, void* p);
+// create a context; arena / stream / stage are the server's (nullptr: the context owns its own)
+int ctx_create(const lbffs_desc* d, Arena* arena, cudaStream_t stream, float* stage, size_t stage_elems,
+               lbffs_ctx** out);
+// condense the uploaded geometry into flags, boundary words and the special list
+int ctx_commit(lbffs_ctx* c);
+// device bytes a context allocates for lattice d (its special list, at most 4 bytes per cell,
+// included), rounded up per block as the server's arena does
+size_t ctx_footprint(const lbffs_desc& d);
+// kernel arguments of one step reading population copy src and macroscopic copy msrc
+void ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int src, int msrc, StepArgs& a);
+
+}  // namespace lbffs

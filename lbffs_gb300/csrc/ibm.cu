@@ -172,6 +172,8 @@ __global__ void k_ibm_force(IbmArgs a)
     const BoxIter bi = box_iter(a.box);
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < bi.n; t += (long long)gridDim.x * blockDim.x) {
         const long long ic = box_cell(bi, t, a.nx, a.ny);
+        const int ip = a.porg + (bi.lo[2] + (int)(t / ((long long)bi.bx * bi.by))) * a.pxy +
+                       (bi.lo[1] + (int)((t / bi.bx) % bi.by)) * a.px + bi.lo[0] + (int)(t % bi.bx);
         const float g[3] = {(float)a.acc[ic], (float)a.acc[a.E + ic], (float)a.acc[2 * a.E + ic]};
         a.acc[ic] = 0.0;
         a.acc[a.E + ic] = 0.0;
@@ -184,7 +186,7 @@ __global__ void k_ibm_force(IbmArgs a)
 #pragma unroll
             for (int q = 0; q < Q; q++) {
                 const float gc = g[0] * (float)lat_c(Q, q, 0) + g[1] * (float)lat_c(Q, q, 1) + g[2] * (float)lat_c(Q, q, 2);
-                T* p = f + (long long)q * a.E + ic;
+                T* p = f + (long long)q * a.pE + ip;
                 const float w = lat_w(Q, q);
                 float v;
                 if constexpr (S == ST_FP32) v = *p;

@@ -25,7 +25,9 @@ struct IbmArgs {
     long long E;
     const float *u, *v, *w, *rho;  // this step's macroscopics
     const uint8_t* flags;
-    void* f_out;                   // this step's post-collision populations
+    void* f_out;                   // this step's post-collision populations (padded planes)
+    int px, pxy, porg;             // padded plane geometry: cell (i,j,k) at porg + k*pxy + j*px + i
+    long long pE;
     float *gx, *gy, *gz;           // Eulerian forcing field (GxIBM..)
 };
 

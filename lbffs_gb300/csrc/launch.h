@@ -24,24 +24,30 @@ cudaError_t setup_pack_bc(const int* boundary, const int* b1, const int* b2, con
 cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
                            const float* omega, float omega0, float cs, uint8_t* flags, uint8_t* scratch, int nx, int ny,
                            int nz, cudaStream_t st);
-// counts[nblocks] of FL_SPECIAL cells per chunk of SETUP_CHUNK cells
+// compaction of the fluid cells whose flags intersect mask (FL_SPECIAL: the boundary-kernel list):
+// counts[nblocks] per chunk of SETUP_CHUNK cells, then scatter
 constexpr int SETUP_CHUNK = 256;
-cudaError_t setup_count_special(const uint8_t* flags, long long E, unsigned* counts, cudaStream_t st);
-cudaError_t setup_scatter_special(const uint8_t* flags, long long E, const unsigned long long* offsets,
+cudaError_t setup_count_special(const uint8_t* flags, long long E, uint8_t mask, unsigned* counts, cudaStream_t st);
+cudaError_t setup_scatter_special(const uint8_t* flags, long long E, uint8_t mask, const unsigned long long* offsets,
                                   uint32_t* out, cudaStream_t st);
 cudaError_t setup_link_masks(int Q, const uint32_t* special, long long n, const uint16_t* bc, const uint8_t* solid,
                              const uint8_t* nei, int nx, int ny, int nz, uint32_t* masks, cudaStream_t st);
-cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long start, long long count, long long E,
-                     cudaStream_t st);
-cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long start, long long count, long long E,
-                     cudaStream_t st);
+// rows [row0, row0 + nrows) of the packed population array (Q*ny*nz rows of nx floats) to / from
+// the padded device planes
+cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long row0, long long nrows,
+                     const PadGeom& g, cudaStream_t st);
+cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long row0, long long nrows,
+                     const PadGeom& g, cudaStream_t st);
+// ghost layer of the population planes f (element size tsize): the face streaming of the six faces
+cudaError_t halo_fill(int Q, int tsize, void* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
+                      cudaStream_t st);
 cudaError_t fill_f32(float* p, float v, long long n, cudaStream_t st);
 // FP64 partial sums: force over the listed cells (3 per block), mass over fluid cells (1 per block)
 constexpr int REDUCE_BS = 256;
 cudaError_t reduce_force(const uint32_t* cells, long long n, const float* fx, const float* fy, const float* fz,
                          double* partial, int nblocks, cudaStream_t st);
-cudaError_t reduce_mass(int storage, int Q, const void* f, const uint8_t* flags, long long E, double* partial,
-                        int nblocks, cudaStream_t st);
+cudaError_t reduce_mass(int storage, int Q, const void* f, const uint8_t* flags, long long E, const PadGeom& g,
+                        double* partial, int nblocks, cudaStream_t st);
 
 // lbffs_api.cu: record the message lbffs_last_error(NULL) returns on this thread
 void set_thread_error(const std::string& msg);

@@ -1,14 +1,12 @@
 // C-ABI implementation (include/lbffs_cuda.h): context lifetime, field transfer,
 // geometry commit, the step loop and reductions.  Host code only; kernels live in
-// step_d3q19.cu, step_d3q27.cu, setup.cu and ibm.cu.
+// step_inst.cu / step_dispatch.cu, setup.cu and ibm.cu.
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
-#include "../../include/lbffs_cuda.h"
-#include "ibm.h"
-#include "launch.h"
+#include "ctx.h"
 
 using namespace lbffs;
 
@@ -44,59 +42,6 @@ FieldInfo field_info(int f)
 
 }  // namespace
 
-struct lbffs_ctx {
-    lbffs_desc d{};
-    int Q = 19;
-    long long E = 0;
-    size_t tsize = 4;
-    int nsm = 0;
-    cudaStream_t stream = nullptr;
-    std::string err = "no error";
-
-    void* f[2] = {nullptr, nullptr};
-    int fcur = 0;
-    int* iarr[4] = {nullptr, nullptr, nullptr, nullptr};  // boundary, boundary1..3 as uploaded
-    uint8_t *solid = nullptr, *nei = nullptr, *flags = nullptr;
-    uint16_t* bc = nullptr;
-    float *u0 = nullptr, *v0 = nullptr, *w0 = nullptr, *omega = nullptr, *sdf = nullptr;
-    float* macro[2][5] = {{nullptr}};
-    int mcur = 0;
-    float* fw[3] = {nullptr, nullptr, nullptr};
-    float* g[3] = {nullptr, nullptr, nullptr};
-    uint32_t* special = nullptr;
-    long long n_special = 0;
-    long long counts[4] = {0, 0, 0, 0};
-    float omega0 = 1.f;
-    int sponge_mask = 0;
-    bool dirty = true;
-    int* d_err = nullptr;
-    float* stage = nullptr;
-    size_t stage_elems = 0;
-    double* partial = nullptr;
-    int partial_blocks = 0;
-
-    // IBM
-    int n_markers = 0;
-    float* markers = nullptr;
-    float* gm = nullptr;
-    double* ibm_acc = nullptr;
-    double* ibm_lag = nullptr;
-    int* ibm_box = nullptr;
-    long long* ibm_t = nullptr;
-    IbmMotion motion{};
-
-    // timing
-    bool timing = false;
-    struct Ev {
-        cudaEvent_t a, b;
-        int kind;
-    };
-    std::vector<Ev> pending;
-    std::vector<cudaEvent_t> pool;
-    double ms[3] = {0, 0, 0};
-    long long launches[3] = {0, 0, 0};
-};
-
 static int fail(lbffs_ctx* c, int code, const std::string& msg)
 {
     if (c) c->err = msg;
@@ -106,6 +51,8 @@ static int fail(lbffs_ctx* c, int code, const std::string& msg)
 
 void lbffs::set_thread_error(const std::string& msg) { g_thread_error = msg; }
 
+int lbffs::ctx_fail(lbffs_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
+
 #define CK(call)                                                                                      \
     do {                                                                                              \
         cudaError_t e_ = (call);                                                                      \
@@ -113,12 +60,30 @@ void lbffs::set_thread_error(const std::string& msg) { g_thread_error = msg; }
             return fail(c, LBFFS_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
     } while (0)
 
-template <class T>
-static cudaError_t dalloc(T** p, size_t n)
+cudaError_t lbffs::ctx_alloc_bytes(lbffs_ctx* c, void** p, size_t bytes)
 {
-    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T) + 16);
-    if (e == cudaSuccess) e = cudaMemset(*p, 0, n * sizeof(T) + 16);
+    *p = nullptr;
+    if (c->arena) {
+        *p = c->arena->alloc(bytes);
+        if (!*p) return cudaErrorMemoryAllocation;
+        return cudaMemsetAsync(*p, 0, bytes, c->stream);
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
     return e;
+}
+
+void lbffs::ctx_free(lbffs_ctx* c, void* p)
+{
+    if (!p) return;
+    if (c->arena && c->arena->owns(p)) c->arena->release(p);
+    else cudaFree(p);
+}
+
+template <class T>
+static cudaError_t dalloc(lbffs_ctx* c, T** p, size_t n)
+{
+    return ctx_alloc(c, p, n);
 }
 
 static size_t field_bytes(const lbffs_ctx* c, int f)
@@ -170,24 +135,24 @@ extern "C" int lbffs_destroy(lbffs_ctx* c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* ptrs[] = {c->f[0], c->f[1], c->iarr[0], c->iarr[1], c->iarr[2], c->iarr[3], c->solid, c->nei, c->flags,
                     c->bc, c->u0, c->v0, c->w0, c->omega, c->sdf, c->fw[0], c->fw[1], c->fw[2], c->g[0], c->g[1],
-                    c->g[2], c->special, c->d_err, c->stage, c->partial, c->markers, c->gm, c->ibm_acc, c->ibm_lag,
-                    c->ibm_box, c->ibm_t};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
+                    c->g[2], c->special, c->d_err, c->partial, c->markers, c->gm, c->ibm_acc,
+                    c->ibm_lag, c->ibm_box, c->ibm_t};
+    for (void* p : ptrs) ctx_free(c, p);
+    if (c->own_stage) ctx_free(c, c->stage);
     for (auto& row : c->macro)
-        for (float* p : row)
-            if (p) cudaFree(p);
+        for (float* p : row) ctx_free(c, p);
     for (auto& e : c->pending) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
     }
     for (auto e : c->pool) cudaEventDestroy(e);
-    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBFFS_OK;
 }
 
-extern "C" int lbffs_create(const lbffs_desc* desc, lbffs_ctx** out)
+int lbffs::ctx_create(const lbffs_desc* desc, Arena* arena, cudaStream_t stream, float* stage, size_t stage_elems,
+                      lbffs_ctx** out)
 {
     lbffs_ctx* c = nullptr;
     if (!desc || !out) return fail(c, LBFFS_E_ARG, "lbffs_create: null argument");
@@ -206,12 +171,21 @@ extern "C" int lbffs_create(const lbffs_desc* desc, lbffs_ctx** out)
     if (!(d.cs > 0.f)) return fail(c, LBFFS_E_ARG, "lbffs_create: cs must be > 0");
     const long long E = (long long)d.nx * d.ny * d.nz;
     if (E >= (1LL << 31)) return fail(c, LBFFS_E_ARG, "lbffs_create: more than 2^31 - 1 cells");
+    // padded planes: one ghost cell on every side, rows starting on 32-byte sectors
+    const int tsize = d.storage == LBFFS_FP32 ? 4 : 2;
+    const long long A = 32 / tsize;
+    const long long px = ((A + d.nx + 1 + A - 1) / A) * A;
+    const long long pxy = px * (d.ny + 2), pE = pxy * (d.nz + 2);
+    if (pE >= (1LL << 31))
+        return fail(c, LBFFS_E_ARG, "lbffs_create: more than 2^31 - 1 cells including the ghost layer");
 
     c = new lbffs_ctx();
     c->d = d;
     c->Q = d.q;
     c->E = E;
-    c->tsize = d.storage == LBFFS_FP32 ? 4 : 2;
+    c->tsize = tsize;
+    c->pg = PadGeom{d.nx, d.ny, d.nz, (int)px, (int)pxy, (int)(pxy + px + A), pE};
+    c->arena = arena;
     cudaError_t e = cudaSetDevice(d.device);
     if (e != cudaSuccess) {
         int r = fail(c, LBFFS_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
@@ -231,39 +205,116 @@ extern "C" int lbffs_create(const lbffs_desc* desc, lbffs_ctx** out)
             return r_;                                                                                     \
         }                                                                                                  \
     } while (0)
-    CKC(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    if (stream) {
+        c->stream = stream;
+        c->own_stream = false;
+    } else {
+        CKC(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    }
     const size_t qe = (size_t)c->Q * (size_t)E;
-    for (int b = 0; b < 2; b++) {
-        CKC(cudaMalloc(&c->f[b], qe * c->tsize + 16));
-        CKC(cudaMemset(c->f[b], 0, qe * c->tsize + 16));
-    }
-    for (int b = 0; b < 4; b++) CKC(dalloc(&c->iarr[b], E));
-    CKC(dalloc(&c->solid, E));
-    CKC(dalloc(&c->nei, E));
-    CKC(dalloc(&c->flags, E));
-    CKC(dalloc(&c->bc, E));
-    CKC(dalloc(&c->u0, E));
-    CKC(dalloc(&c->v0, E));
-    CKC(dalloc(&c->w0, E));
-    CKC(dalloc(&c->omega, E));
-    CKC(dalloc(&c->sdf, E));
+    const size_t qpe = (size_t)c->Q * (size_t)pE;
+    for (int b = 0; b < 2; b++) CKC(ctx_alloc_bytes(c, &c->f[b], qpe * c->tsize + 16));
+    for (int b = 0; b < 4; b++) CKC(dalloc(c, &c->iarr[b], E));
+    CKC(dalloc(c, &c->solid, E));
+    CKC(dalloc(c, &c->nei, E));
+    CKC(dalloc(c, &c->flags, E));
+    CKC(dalloc(c, &c->bc, E));
+    CKC(dalloc(c, &c->u0, E));
+    CKC(dalloc(c, &c->v0, E));
+    CKC(dalloc(c, &c->w0, E));
+    CKC(dalloc(c, &c->omega, E));
+    CKC(dalloc(c, &c->sdf, E));
     for (auto& row : c->macro)
-        for (float*& p : row) CKC(dalloc(&p, E));
-    for (int a = 0; a < 3; a++) {
-        CKC(dalloc(&c->fw[a], E));
-        CKC(dalloc(&c->g[a], E));
+        for (float*& p : row) CKC(dalloc(c, &p, E));
+    for (int a = 0; a < 3; a++) CKC(dalloc(c, &c->fw[a], E));
+    CKC(dalloc(c, &c->d_err, 1));
+    if (stage) {
+        c->stage = stage;
+        c->stage_elems = stage_elems;
+        c->own_stage = false;
+    } else {
+        c->stage_elems = (size_t)16 << 20;  // 64 MB float staging for population conversion, whole rows
+        if (c->stage_elems < (size_t)d.nx) c->stage_elems = (size_t)d.nx;
+        if (c->stage_elems > qe) c->stage_elems = qe;
+        CKC(dalloc(c, &c->stage, c->stage_elems));
     }
-    CKC(dalloc(&c->d_err, 1));
-    c->stage_elems = (size_t)16 << 20;  // 64 MB float staging for population conversion
-    if (c->stage_elems > qe) c->stage_elems = qe;
-    CKC(dalloc(&c->stage, c->stage_elems));
     c->partial_blocks = 4 * c->nsm;
-    CKC(dalloc(&c->partial, (size_t)3 * c->partial_blocks));
+    CKC(dalloc(c, &c->partial, (size_t)3 * c->partial_blocks));
     CKC(fill_f32(c->sdf, 10000.f, E, c->stream));
     CKC(fill_f32(c->omega, 1.f, E, c->stream));
     CKC(cudaStreamSynchronize(c->stream));
 #undef CKC
     *out = c;
+    return LBFFS_OK;
+}
+
+size_t lbffs::ctx_footprint(const lbffs_desc& d)
+{
+    const size_t E = (size_t)d.nx * d.ny * d.nz;
+    const size_t tsize = d.storage == LBFFS_FP32 ? 4 : 2;
+    const size_t A = 32 / tsize;
+    const size_t px = ((A + d.nx + 1 + A - 1) / A) * A;
+    const size_t pE = px * (d.ny + 2) * (d.nz + 2);
+    auto blk = [](size_t b) { return (b + 16 + Arena::kAlign - 1) / Arena::kAlign * Arena::kAlign; };
+    size_t t = 2 * blk((size_t)d.q * pE * tsize);
+    t += 4 * blk(4 * E);                       // boundary codes
+    t += 3 * blk(E) + blk(2 * E);              // solid, neiSolid, flags, bc
+    t += 5 * blk(4 * E);                       // u0, v0, w0, omega, sdf
+    t += 10 * blk(4 * E) + 3 * blk(4 * E);     // macroscopics x 2, Fw
+    t += blk(4 * E) + blk(E);                  // special list (worst case), classify scratch
+    t += blk(64 * 1024);                       // error word, partial sums, compaction counters
+    return t;
+}
+
+extern "C" int lbffs_create(const lbffs_desc* desc, lbffs_ctx** out)
+{
+    return ctx_create(desc, nullptr, nullptr, nullptr, 0, out);
+}
+
+// IBM forcing fields (GxIBM..), allocated when markers or an upload first need them
+static cudaError_t ensure_g(lbffs_ctx* c)
+{
+    for (int a = 0; a < 3; a++)
+        if (!c->g[a]) {
+            cudaError_t e = dalloc(c, &c->g[a], c->E);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
+// Compact list (ascending cell order) of the fluid cells whose flags intersect mask.
+static int build_list(lbffs_ctx* c, uint8_t mask, uint32_t** list, long long* n)
+{
+    const long long E = c->E;
+    const long long nb = (E + SETUP_CHUNK - 1) / SETUP_CHUNK;
+    unsigned* d_counts = nullptr;
+    unsigned long long* d_off = nullptr;
+    CK(ctx_alloc_bytes(c, (void**)&d_counts, sizeof(unsigned) * nb));
+    cudaError_t e = setup_count_special(c->flags, E, mask, d_counts, c->stream);
+    std::vector<unsigned> counts(nb);
+    std::vector<unsigned long long> off(nb);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(counts.data(), d_counts, sizeof(unsigned) * nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    unsigned long long total = 0;
+    for (long long b = 0; b < nb; b++) {
+        off[b] = total;
+        total += counts[b];
+    }
+    if (e == cudaSuccess) e = ctx_alloc_bytes(c, (void**)&d_off, sizeof(unsigned long long) * nb);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_off, off.data(), sizeof(unsigned long long) * nb, cudaMemcpyHostToDevice, c->stream);
+    if (*list) {
+        ctx_free(c, *list);
+        *list = nullptr;
+    }
+    if (e == cudaSuccess) e = ctx_alloc_bytes(c, (void**)list, sizeof(uint32_t) * (total + 1));
+    if (e == cudaSuccess) e = setup_scatter_special(c->flags, E, mask, d_off, *list, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    ctx_free(c, d_counts);
+    ctx_free(c, d_off);
+    CK(e);
+    *n = (long long)total;
     return LBFFS_OK;
 }
 
@@ -304,42 +355,17 @@ static int commit(lbffs_ctx* c)
 
     CK(setup_pack_bc(c->iarr[0], c->iarr[1], c->iarr[2], c->iarr[3], c->bc, nx, ny, nz, c->stream));
     uint8_t* scratch = nullptr;
-    CK(cudaMalloc(&scratch, E));
+    CK(ctx_alloc_bytes(c, (void**)&scratch, E));
     cudaError_t e = setup_classify(c->Q, c->bc, c->solid, c->nei, c->sdf, c->omega, c->omega0, c->d.cs, c->flags,
                                    scratch, nx, ny, nz, c->stream);
     cudaStreamSynchronize(c->stream);
-    cudaFree(scratch);
+    ctx_free(c, scratch);
     CK(e);
 
-    const long long nb = (E + SETUP_CHUNK - 1) / SETUP_CHUNK;
-    unsigned* d_counts = nullptr;
-    unsigned long long* d_off = nullptr;
-    CK(cudaMalloc(&d_counts, sizeof(unsigned) * nb));
-    e = setup_count_special(c->flags, E, d_counts, c->stream);
-    std::vector<unsigned> counts(nb);
-    std::vector<unsigned long long> off(nb);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(counts.data(), d_counts, sizeof(unsigned) * nb, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    unsigned long long total = 0;
-    for (long long b = 0; b < nb; b++) {
-        off[b] = total;
-        total += counts[b];
+    {
+        int r = build_list(c, FL_SPECIAL, &c->special, &c->n_special);
+        if (r != LBFFS_OK) return r;
     }
-    if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(unsigned long long) * nb);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_off, off.data(), sizeof(unsigned long long) * nb, cudaMemcpyHostToDevice, c->stream);
-    if (c->special) {
-        cudaFree(c->special);
-        c->special = nullptr;
-    }
-    if (e == cudaSuccess) e = cudaMalloc(&c->special, sizeof(uint32_t) * (total + 1));
-    if (e == cudaSuccess) e = setup_scatter_special(c->flags, E, d_off, c->special, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cudaFree(d_counts);
-    if (d_off) cudaFree(d_off);
-    CK(e);
-    c->n_special = (long long)total;
 
     // per-class counts and zeroed link forces
     std::vector<uint8_t> fl(E);
@@ -374,15 +400,16 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
     CK(cudaSetDevice(c->d.device));
     FieldInfo fi = field_info(field);
     if (fi.kind == K_F) {
-        const size_t total = (size_t)c->Q * (size_t)c->E;
+        const long long nx = c->d.nx;
+        const long long rows = (long long)c->Q * c->d.ny * c->d.nz, chunk = (long long)c->stage_elems / nx;
         const float* h = static_cast<const float*>(host);
         // both population copies get the uploaded values: initialization.hpp fills f and fTmp alike, and
         // cells that are never written (solid cells) must read the same values from either copy
-        for (size_t s = 0; s < total; s += c->stage_elems) {
-            const size_t n = (total - s < c->stage_elems) ? total - s : c->stage_elems;
-            CK(cudaMemcpyAsync(c->stage, h + s, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-            for (int b = 0; b < 2; b++)
-                CK(encode_f(c->d.storage, c->Q, c->stage, c->f[b], (long long)s, (long long)n, c->E, c->stream));
+        for (long long r = 0; r < rows; r += chunk) {
+            const long long n = (rows - r < chunk) ? rows - r : chunk;
+            CK(cudaMemcpyAsync(c->stage, h + r * nx, (size_t)(n * nx) * sizeof(float), cudaMemcpyHostToDevice,
+                               c->stream));
+            for (int b = 0; b < 2; b++) CK(encode_f(c->d.storage, c->Q, c->stage, c->f[b], r, n, c->pg, c->stream));
         }
         CK(cudaStreamSynchronize(c->stream));
         return LBFFS_OK;
@@ -393,6 +420,7 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
         CK(cudaStreamSynchronize(c->stream));
         return LBFFS_OK;
     }
+    if (field == LBFFS_GXIBM || field == LBFFS_GYIBM || field == LBFFS_GZIBM) CK(ensure_g(c));
     void* p = field_ptr(c, field);
     CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -408,17 +436,23 @@ extern "C" int lbffs_download(lbffs_ctx* c, int field, void* host, size_t bytes)
     CK(cudaSetDevice(c->d.device));
     FieldInfo fi = field_info(field);
     if (fi.kind == K_F) {
-        const size_t total = (size_t)c->Q * (size_t)c->E;
+        const long long nx = c->d.nx;
+        const long long rows = (long long)c->Q * c->d.ny * c->d.nz, chunk = (long long)c->stage_elems / nx;
         float* h = static_cast<float*>(host);
-        for (size_t s = 0; s < total; s += c->stage_elems) {
-            const size_t n = (total - s < c->stage_elems) ? total - s : c->stage_elems;
-            CK(decode_f(c->d.storage, c->Q, c->f[c->fcur], c->stage, (long long)s, (long long)n, c->E, c->stream));
-            CK(cudaMemcpyAsync(h + s, c->stage, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        for (long long r = 0; r < rows; r += chunk) {
+            const long long n = (rows - r < chunk) ? rows - r : chunk;
+            CK(decode_f(c->d.storage, c->Q, c->f[c->fcur], c->stage, r, n, c->pg, c->stream));
+            CK(cudaMemcpyAsync(h + r * nx, c->stage, (size_t)(n * nx) * sizeof(float), cudaMemcpyDeviceToHost,
+                               c->stream));
             CK(cudaStreamSynchronize(c->stream));
         }
         return LBFFS_OK;
     }
     const void* p = fi.kind == K_MACRO ? c->macro[c->mcur][fi.macro] : field_ptr(c, field);
+    if (!p) {  // IBM forcing fields before any marker was set: zero
+        memset(host, 0, bytes);
+        return LBFFS_OK;
+    }
     CK(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return LBFFS_OK;
@@ -450,16 +484,11 @@ static void harvest_timing(lbffs_ctx* c)
     c->pending.clear();
 }
 
-extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
+int lbffs::ctx_commit(lbffs_ctx* c) { return commit(c); }
+
+void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int src, int msrc, StepArgs& a)
 {
-    if (!c || !p) return fail(c, LBFFS_E_ARG, "lbffs_step: null argument");
-    if (nsteps < 0) return fail(c, LBFFS_E_ARG, "lbffs_step: nsteps < 0");
-    CK(cudaSetDevice(c->d.device));
-    if (c->dirty) {
-        int r = commit(c);
-        if (r != LBFFS_OK) return r;
-    }
-    StepArgs a{};
+    a = StepArgs{};
     a.flags = c->flags;
     a.bc = c->bc;
     a.solid = c->solid;
@@ -491,36 +520,75 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
     a.sponge_mask = c->sponge_mask;
     a.sgs = c->d.sgs;
     a.wall = c->d.wall;
-    {
-        const long long sz = (c->d.nz > 1) ? (long long)c->d.nx * c->d.ny : 0;
-        for (int q = 0; q < c->Q; q++)
-            a.pull_off[q] = (int)(lat_c(c->Q, q, 0) + (long long)lat_c(c->Q, q, 1) * c->d.nx + lat_c(c->Q, q, 2) * sz);
-    }
+    a.px = c->pg.px;
+    a.pxy = c->pg.pxy;
+    a.porg = c->pg.porg;
+    a.pE = c->pg.pE;
     a.ibm_box = c->n_markers > 1 ? c->ibm_box : nullptr;
     a.err = c->d_err;
+    a.f_in = c->f[src];
+    a.f_out = c->f[1 - src];
+    for (int q = 0; q < c->Q; q++) {
+        const long long pull =
+            lat_c(c->Q, q, 0) + (long long)lat_c(c->Q, q, 1) * a.px + (long long)lat_c(c->Q, q, 2) * a.pxy;
+        const size_t plane = (size_t)q * (size_t)a.pE * c->tsize;
+        a.fin_q[q] = static_cast<const char*>(a.f_in) + plane;
+        // plane base moved back by the pull offset; every address formed from it is inside the plane
+        a.fin_s[q] = reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(a.fin_q[q]) -
+                                                   (uintptr_t)(pull * (long long)c->tsize));
+        a.fout_q[q] = static_cast<char*>(a.f_out) + plane;
+        a.pull_b[q] = (long long)plane - pull * (long long)c->tsize;
+        a.plane_b[q] = (long long)plane;
+    }
+    a.fin_base = static_cast<const char*>(a.f_in);
+    a.fout_base = static_cast<char*>(a.f_out);
+    float* const* mp = c->macro[msrc];
+    float* const* mn = c->macro[1 - msrc];
+    a.rho_p = mp[0];
+    a.u_p = mp[1];
+    a.v_p = mp[2];
+    a.w_p = mp[3];
+    a.tau_p = mp[4];
+    a.rho_n = mn[0];
+    a.u_n = mn[1];
+    a.v_n = mn[2];
+    a.w_n = mn[3];
+    a.tau_n = mn[4];
+    a.store_all = p->store_fields == 2;
+}
+
+extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
+{
+    if (!c || !p) return fail(c, LBFFS_E_ARG, "lbffs_step: null argument");
+    if (nsteps < 0) return fail(c, LBFFS_E_ARG, "lbffs_step: nsteps < 0");
+    CK(cudaSetDevice(c->d.device));
+    if (c->dirty) {
+        int r = commit(c);
+        if (r != LBFFS_OK) return r;
+    }
     StepConfig cfg{c->d.storage, c->d.collision, c->d.sgs, c->d.wall,
                    c->d.sgs == LBFFS_SGS_SMAGORINSKY && p->les != 0.f};
     auto launch = (c->Q == 19) ? launch_q19 : launch_q27;
     for (int s = 0; s < nsteps; s++) {
-        a.f_in = c->f[c->fcur];
-        a.f_out = c->f[1 - c->fcur];
-        for (int q = 0; q < c->Q; q++) {
-            a.fin_q[q] = static_cast<const char*>(a.f_in) + (size_t)q * (size_t)c->E * c->tsize;
-            a.fout_q[q] = static_cast<char*>(a.f_out) + (size_t)q * (size_t)c->E * c->tsize;
-        }
-        float** mp = c->macro[c->mcur];
-        float** mn = c->macro[1 - c->mcur];
-        a.rho_p = mp[0];
-        a.u_p = mp[1];
-        a.v_p = mp[2];
-        a.w_p = mp[3];
-        a.tau_p = mp[4];
-        a.rho_n = mn[0];
-        a.u_n = mn[1];
-        a.v_n = mn[2];
-        a.w_n = mn[3];
-        a.tau_n = mn[4];
+        StepArgs a;
+        ctx_step_args(c, p, c->fcur, c->mcur, a);
         a.store_all = (p->store_fields == 2) || (p->store_fields == 1 && s == nsteps - 1);
+        // ghost layer of this step's source populations: the face streaming of the six faces
+        {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (c->timing) {
+                e0 = get_event(c);
+                e1 = get_event(c);
+                cudaEventRecord(e0, c->stream);
+            }
+            cudaError_t e = halo_fill(c->Q, (int)c->tsize, c->f[c->fcur], c->flags, c->bc, c->pg, c->stream);
+            if (c->timing) {
+                cudaEventRecord(e1, c->stream);
+                c->pending.push_back({e0, e1, 3});
+            }
+            if (e != cudaSuccess) return fail(c, LBFFS_E_CUDA, std::string("halo launch: ") + cudaGetErrorString(e));
+        }
+        float** mn = c->macro[1 - c->mcur];
         for (int half = 0; half < 2; half++) {
             const bool bulk = half == 0;
             if (!bulk && c->n_special == 0) continue;
@@ -557,6 +625,10 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
             ia.rho = mn[0];
             ia.flags = c->flags;
             ia.f_out = a.f_out;
+            ia.px = a.px;
+            ia.pxy = a.pxy;
+            ia.porg = a.porg;
+            ia.pE = a.pE;
             ia.gx = c->g[0];
             ia.gy = c->g[1];
             ia.gz = c->g[2];
@@ -616,7 +688,7 @@ extern "C" int lbffs_mass(lbffs_ctx* c, double* out)
         if (r != LBFFS_OK) return r;
     }
     const int nb = c->partial_blocks;
-    CK(reduce_mass(c->d.storage, c->Q, c->f[c->fcur], c->flags, c->E, c->partial, nb, c->stream));
+    CK(reduce_mass(c->d.storage, c->Q, c->f[c->fcur], c->flags, c->E, c->pg, c->partial, nb, c->stream));
     std::vector<double> h(nb);
     CK(cudaMemcpyAsync(h.data(), c->partial, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -637,7 +709,7 @@ extern "C" int lbffs_links(lbffs_ctx* c, long long* cells, unsigned* masks, long
     *n = 0;
     if (c->n_special == 0) return LBFFS_OK;
     uint32_t* d_masks = nullptr;
-    CK(cudaMalloc(&d_masks, sizeof(uint32_t) * c->n_special));
+    CK(ctx_alloc_bytes(c, (void**)&d_masks, sizeof(uint32_t) * c->n_special + 16));
     cudaError_t e = setup_link_masks(c->Q, c->special, c->n_special, c->bc, c->solid, c->nei, c->d.nx, c->d.ny,
                                      c->d.nz, d_masks, c->stream);
     std::vector<uint32_t> hm(c->n_special), hc(c->n_special);
@@ -646,7 +718,7 @@ extern "C" int lbffs_links(lbffs_ctx* c, long long* cells, unsigned* masks, long
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(hc.data(), c->special, sizeof(uint32_t) * c->n_special, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    cudaFree(d_masks);
+    ctx_free(c, d_masks);
     CK(e);
     long long k = 0;
     for (long long t = 0; t < c->n_special; t++) {
@@ -666,19 +738,19 @@ extern "C" int lbffs_set_markers(lbffs_ctx* c, const float* xyz, int n)
     if (!c || (n > 0 && !xyz) || n < 0) return fail(c, LBFFS_E_ARG, "lbffs_set_markers: bad argument");
     CK(cudaSetDevice(c->d.device));
     CK(cudaStreamSynchronize(c->stream));
-    if (c->markers) cudaFree(c->markers);
-    if (c->gm) cudaFree(c->gm);
-    c->markers = nullptr;
-    c->gm = nullptr;
+    ctx_free(c, c->markers);
+    ctx_free(c, c->gm);
+    c->markers = c->gm = nullptr;
     c->n_markers = n;
     if (n == 0) return LBFFS_OK;
-    CK(dalloc(&c->markers, (size_t)3 * n));
-    CK(dalloc(&c->gm, (size_t)3 * n));
+    CK(ensure_g(c));
+    CK(dalloc(c, &c->markers, (size_t)3 * n));
+    CK(dalloc(c, &c->gm, (size_t)3 * n));
     CK(cudaMemcpy(c->markers, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
-    if (!c->ibm_acc) CK(dalloc(&c->ibm_acc, (size_t)3 * c->E));
-    if (!c->ibm_lag) CK(dalloc(&c->ibm_lag, 3));
-    if (!c->ibm_box) CK(dalloc(&c->ibm_box, 12));
-    if (!c->ibm_t) CK(dalloc(&c->ibm_t, 1));
+    if (!c->ibm_acc) CK(dalloc(c, &c->ibm_acc, (size_t)3 * c->E));
+    if (!c->ibm_lag) CK(dalloc(c, &c->ibm_lag, 3));
+    if (!c->ibm_box) CK(dalloc(c, &c->ibm_box, 12));
+    if (!c->ibm_t) CK(dalloc(c, &c->ibm_t, 1));
     IbmArgs ia{};
     ia.markers = c->markers;
     ia.box = c->ibm_box;
@@ -763,7 +835,11 @@ extern "C" int lbffs_set_timing(lbffs_ctx* c, int enabled)
 extern "C" int lbffs_kernel_time(lbffs_ctx* c, const char* name, double* total_ms, long long* launches)
 {
     if (!c || !name || !total_ms || !launches) return fail(c, LBFFS_E_ARG, "lbffs_kernel_time: null argument");
-    int k = !strcmp(name, "bulk") ? 0 : !strcmp(name, "special") ? 1 : !strcmp(name, "ibm") ? 2 : -1;
+    int k = !strcmp(name, "bulk")      ? 0
+            : !strcmp(name, "special") ? 1
+            : !strcmp(name, "ibm")     ? 2
+            : !strcmp(name, "halo")    ? 3
+                                       : -1;
     if (k < 0) return fail(c, LBFFS_E_ARG, "lbffs_kernel_time: unknown kernel name");
     CK(cudaSetDevice(c->d.device));
     CK(cudaStreamSynchronize(c->stream));
@@ -782,5 +858,24 @@ extern "C" int lbffs_cell_counts(lbffs_ctx* c, long long out[4])
         if (r != LBFFS_OK) return r;
     }
     for (int k = 0; k < 4; k++) out[k] = c->counts[k];
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_init_rest(lbffs_ctx* c)
+{
+    if (!c) return fail(c, LBFFS_E_ARG, "lbffs_init_rest: null context");
+    CK(cudaSetDevice(c->d.device));
+    const size_t plane_bytes = (size_t)c->pg.pE * c->tsize;
+    for (int b = 0; b < 2; b++) {
+        if (c->d.storage == LBFFS_FP32) {
+            for (int q = 0; q < c->Q; q++)
+                CK(fill_f32(reinterpret_cast<float*>(static_cast<char*>(c->f[b]) + q * plane_bytes), lat_w(c->Q, q),
+                            c->pg.pE, c->stream));
+        } else {
+            // shifted storage holds f - w = 0
+            CK(cudaMemsetAsync(c->f[b], 0, plane_bytes * c->Q, c->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(c->stream));
     return LBFFS_OK;
 }

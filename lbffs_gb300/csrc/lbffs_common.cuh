@@ -2,8 +2,16 @@
 // storage codecs, per-cell flag bits and the kernel argument block.
 //
 // Data layout in HBM (one context = one lattice):
-//   populations   f[q*E + ic], ic = (k*ny + j)*nx + i, two copies (pull ping-pong),
-//                 each element float (FP32), or a shifted/scaled half / bfloat16
+//   populations   two copies (pull ping-pong) of Q planes; each plane is the grid with a
+//                 one-cell ghost layer on every side, rows padded so that every row of
+//                 interior cells starts on a 32-byte sector: cell (i,j,k) lives at
+//                 ip = porg + k*pxy + j*px + i of plane q (plane stride pE).  Elements are
+//                 float (FP32), or a shifted/scaled half / bfloat16.  The ghost layer holds,
+//                 for each population that crosses the domain border, the value the
+//                 reference's face streaming would pull (wrap, bounce-back or mirror), so
+//                 every cell pulls population q from ip - (c_x + c_y*px + c_z*pxy).
+//   cell arrays   everything else is indexed by ic = (k*ny + j)*nx + i (the reference's
+//                 own layout, src/base.hpp:20)
 //   flags         u8 per cell (FL_* bits below), built on the device from the
 //                 reference's boundary/solid/neiSolid/sdf/omega arrays
 //   bc            u16 per cell: boundary1 | boundary2<<3 | boundary3<<6 | face<<9
@@ -34,7 +42,11 @@ constexpr uint8_t FL_STORE = 4;    // macroscopics are read by a neighbour next 
 constexpr uint8_t FL_SDF = 8;      // near-wall damping factor < 1: read sdf
 constexpr uint8_t FL_OMEGA = 16;   // omega differs from the uniform omega0: read omega[]
 constexpr uint8_t FL_LINK = 32;    // has at least one STL link
-constexpr uint8_t FL_FACE = 64;    // on the domain border
+constexpr uint8_t FL_FACE = 64;    // on the domain border (face codes apply)
+
+// bulk kernel tiling: BULK_BX threads per block, BULK_V cells per thread (32 apart)
+constexpr int BULK_BX = 128;
+constexpr int BULK_V = 2;
 
 constexpr float FP16S_SCALE = 32768.0f;  // (f - w) * 2^15 keeps |f - w| < 2 in range, 1.9e-9 above subnormals
 constexpr float FP16S_INV = 1.0f / 32768.0f;
@@ -87,8 +99,9 @@ struct Codec<ST_FP32> {
     using T = float;
     static __device__ __forceinline__ float load(const T* p, float) { return __ldg(p); }
     static __device__ __forceinline__ void store(T* p, float v, float) { __stcs(p, v); }
-    // held value in the bulk kernel: f itself (DEV = false)
+    // held value in the bulk kernel: f itself (DEV = false), unscaled (HS = 1)
     static constexpr bool DEV = false;
+    static constexpr int HS = 1;
     static __device__ __forceinline__ float load_held(const T* p) { return __ldg(p); }
     static __device__ __forceinline__ void store_held(T* p, float v) { __stcs(p, v); }
 };
@@ -105,10 +118,13 @@ struct Codec<ST_FP16S> {
     {
         *p = __float2half_rn((v - w) * FP16S_SCALE);
     }
-    // held value in the bulk kernel: the deviation g = f - w itself (DEV = true)
+    // held value in the bulk kernel: the stored number itself, 2^15 (f - w) (DEV = true,
+    // HS = 2^15); the collision folds the power-of-two scale into its constants, which
+    // leaves every rounding unchanged
     static constexpr bool DEV = true;
-    static __device__ __forceinline__ float load_held(const T* p) { return __half2float(__ldg(p)) * FP16S_INV; }
-    static __device__ __forceinline__ void store_held(T* p, float g) { *p = __float2half_rn(g * FP16S_SCALE); }
+    static constexpr int HS = 32768;
+    static __device__ __forceinline__ float load_held(const T* p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ void store_held(T* p, float gs) { *p = __float2half_rn(gs); }
 };
 
 // BF16S: bfloat16 of (f - w_q); arithmetic stays FP32.
@@ -118,9 +134,22 @@ struct Codec<ST_BF16S> {
     static __device__ __forceinline__ float load(const T* p, float w) { return __bfloat162float(__ldg(p)) + w; }
     static __device__ __forceinline__ void store(T* p, float v, float w) { *p = __float2bfloat16_rn(v - w); }
     static constexpr bool DEV = true;
+    static constexpr int HS = 1;
     static __device__ __forceinline__ float load_held(const T* p) { return __bfloat162float(__ldg(p)); }
     static __device__ __forceinline__ void store_held(T* p, float g) { *p = __float2bfloat16_rn(g); }
 };
+
+// Padded population planes: cell (i,j,k) at porg + k*pxy + j*px + i of a plane of pE elements.
+struct PadGeom {
+    int nx, ny, nz, px, pxy, porg;
+    long long pE;
+};
+
+// threads of one ghost-layer fill: one per cell of each of the six faces
+__host__ __device__ inline long long halo_threads(const PadGeom& g)
+{
+    return 2LL * ((long long)g.ny * g.nz + (long long)g.nx * g.nz + (long long)g.nx * g.ny);
+}
 
 // ---- kernel argument block ----
 struct StepArgs {
@@ -145,12 +174,27 @@ struct StepArgs {
     int sgs, wall;    // Sgs / Wall selections (runtime in the boundary kernel)
     const int* ibm_box;  // device int[6] lo/hi of the marker box (cells inside store macroscopics), or null
     int* err;            // device error word (non-finite density seen), may be null
-    // per-direction plane bases and pull offsets: population q of cell ic is read at
-    // fin_q[q][ic - pull_off[q]] and written at fout_q[q][ic]; cell indices fit in 32 bits
+    // padded population planes: cell (i,j,k) at ip = porg + k*pxy + j*px + i (< 2^31)
+    int px, pxy, porg;
+    long long pE;
+    // per-direction plane bases: fin_q[q][ip] is the cell's own value of population q,
+    // fin_s[q][ip] the value it pulls (the plane base moved by the pull offset), and
+    // fout_q[q][ip] where it writes
     const void* fin_q[27];
+    const void* fin_s[27];
     void* fout_q[27];
-    int pull_off[27];
+    // the same as byte offsets from one base per copy, for the bulk kernel's single row pointer:
+    // pulled value fin_base + ip*size + pull_b[q], own output fout_base + ip*size + plane_b[q]
+    const char* fin_base;
+    char* fout_base;
+    long long pull_b[27];
+    long long plane_b[27];
 };
+
+__host__ __device__ __forceinline__ int pidx(const StepArgs& a, int i, int j, int k)
+{
+    return a.porg + k * a.pxy + j * a.px + i;
+}
 
 __device__ __forceinline__ bool in_box(const StepArgs& a, int i, int j, int k)
 {

@@ -113,26 +113,27 @@ cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, cons
     return cudaGetLastError();
 }
 
-__global__ void k_count_special(const uint8_t* flags, long long E, unsigned* counts)
+__global__ void k_count_special(const uint8_t* flags, long long E, uint8_t mask, unsigned* counts)
 {
     const long long ic = (long long)blockIdx.x * SETUP_CHUNK + threadIdx.x;
-    const bool sp = ic < E && (flags[ic] & FL_SPECIAL);
+    const bool sp = ic < E && (flags[ic] & mask) && !(flags[ic] & FL_SOLID);
     const int n = __syncthreads_count(sp);
     if (threadIdx.x == 0) counts[blockIdx.x] = (unsigned)n;
 }
 
-cudaError_t setup_count_special(const uint8_t* flags, long long E, unsigned* counts, cudaStream_t st)
+cudaError_t setup_count_special(const uint8_t* flags, long long E, uint8_t mask, unsigned* counts, cudaStream_t st)
 {
     const unsigned nb = (unsigned)((E + SETUP_CHUNK - 1) / SETUP_CHUNK);
-    k_count_special<<<nb, SETUP_CHUNK, 0, st>>>(flags, E, counts);
+    k_count_special<<<nb, SETUP_CHUNK, 0, st>>>(flags, E, mask, counts);
     return cudaGetLastError();
 }
 
-__global__ void k_scatter_special(const uint8_t* flags, long long E, const unsigned long long* offsets, uint32_t* out)
+__global__ void k_scatter_special(const uint8_t* flags, long long E, uint8_t mask, const unsigned long long* offsets,
+                                  uint32_t* out)
 {
     __shared__ unsigned warp_base[SETUP_CHUNK / 32];
     const long long ic = (long long)blockIdx.x * SETUP_CHUNK + threadIdx.x;
-    const bool sp = ic < E && (flags[ic] & FL_SPECIAL);
+    const bool sp = ic < E && (flags[ic] & mask) && !(flags[ic] & FL_SOLID);
     const unsigned m = __ballot_sync(0xffffffffu, sp);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) warp_base[warp] = __popc(m);
@@ -152,11 +153,11 @@ __global__ void k_scatter_special(const uint8_t* flags, long long E, const unsig
     }
 }
 
-cudaError_t setup_scatter_special(const uint8_t* flags, long long E, const unsigned long long* offsets, uint32_t* out,
-                                  cudaStream_t st)
+cudaError_t setup_scatter_special(const uint8_t* flags, long long E, uint8_t mask, const unsigned long long* offsets,
+                                  uint32_t* out, cudaStream_t st)
 {
     const unsigned nb = (unsigned)((E + SETUP_CHUNK - 1) / SETUP_CHUNK);
-    k_scatter_special<<<nb, SETUP_CHUNK, 0, st>>>(flags, E, offsets, out);
+    k_scatter_special<<<nb, SETUP_CHUNK, 0, st>>>(flags, E, mask, offsets, out);
     return cudaGetLastError();
 }
 
@@ -194,76 +195,114 @@ cudaError_t setup_link_masks(int Q, const uint32_t* special, long long n, const 
 }
 
 // ---- population format conversion (host float32 layout <-> storage) ----
-template <int S, int Q>
-__global__ void k_encode(const float* src, typename Codec<S>::T* dst, long long start, long long count, long long E)
+// Populations between the reference's packed layout (Q*ny*nz rows of nx values) and the padded
+// device planes, one block per row: rows [row0, row0 + nrows) of the packed array live in src /
+// dst, the device planes in the padded layout of g.
+template <int Q>
+__device__ __forceinline__ float weight_of(int q)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count) return;
-    const long long e = start + t;
-    const int q = (int)(e / E);
     float w = 0.f;
 #pragma unroll
     for (int p = 0; p < Q; p++)
         if (p == q) w = lat_w(Q, p);
-    Codec<S>::store(dst + e, src[t], w);
+    return w;
+}
+
+__device__ __forceinline__ long long padded_row(const PadGeom& g, long long r, int& q)
+{
+    const long long plane_rows = (long long)g.ny * g.nz;
+    q = (int)(r / plane_rows);
+    const long long jk = r - (long long)q * plane_rows;
+    const int j = (int)(jk % g.ny), k = (int)(jk / g.ny);
+    return (long long)q * g.pE + g.porg + (long long)k * g.pxy + (long long)j * g.px;
 }
 
 template <int S, int Q>
-__global__ void k_decode(const typename Codec<S>::T* src, float* dst, long long start, long long count, long long E)
+__global__ void k_encode(const float* src, typename Codec<S>::T* dst, long long row0, PadGeom g)
+{
+    int q;
+    const long long base = padded_row(g, row0 + blockIdx.x, q);
+    const float w = weight_of<Q>(q);
+    const float* s = src + (long long)blockIdx.x * g.nx;
+    for (int i = threadIdx.x; i < g.nx; i += blockDim.x) Codec<S>::store(dst + base + i, s[i], w);
+}
+
+template <int S, int Q>
+__global__ void k_decode(const typename Codec<S>::T* src, float* dst, long long row0, PadGeom g)
+{
+    int q;
+    const long long base = padded_row(g, row0 + blockIdx.x, q);
+    const float w = weight_of<Q>(q);
+    float* d = dst + (long long)blockIdx.x * g.nx;
+    for (int i = threadIdx.x; i < g.nx; i += blockDim.x) d[i] = Codec<S>::load(src + base + i, w);
+}
+
+template <int S>
+static cudaError_t enc_q(int Q, const float* src, void* dst, long long row0, long long nrows, const PadGeom& g,
+                         cudaStream_t st)
+{
+    using T = typename Codec<S>::T;
+    if (Q == 19) k_encode<S, 19><<<(unsigned)nrows, 256, 0, st>>>(src, static_cast<T*>(dst), row0, g);
+    else k_encode<S, 27><<<(unsigned)nrows, 256, 0, st>>>(src, static_cast<T*>(dst), row0, g);
+    return cudaGetLastError();
+}
+
+template <int S>
+static cudaError_t dec_q(int Q, const void* src, float* dst, long long row0, long long nrows, const PadGeom& g,
+                         cudaStream_t st)
+{
+    using T = typename Codec<S>::T;
+    if (Q == 19) k_decode<S, 19><<<(unsigned)nrows, 256, 0, st>>>(static_cast<const T*>(src), dst, row0, g);
+    else k_decode<S, 27><<<(unsigned)nrows, 256, 0, st>>>(static_cast<const T*>(src), dst, row0, g);
+    return cudaGetLastError();
+}
+
+cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long row0, long long nrows,
+                     const PadGeom& g, cudaStream_t st)
+{
+    if (nrows <= 0) return cudaSuccess;
+    switch (storage) {
+        case ST_FP32: return enc_q<ST_FP32>(Q, src, dst, row0, nrows, g, st);
+        case ST_FP16S: return enc_q<ST_FP16S>(Q, src, dst, row0, nrows, g, st);
+        case ST_BF16S: return enc_q<ST_BF16S>(Q, src, dst, row0, nrows, g, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long row0, long long nrows,
+                     const PadGeom& g, cudaStream_t st)
+{
+    if (nrows <= 0) return cudaSuccess;
+    switch (storage) {
+        case ST_FP32: return dec_q<ST_FP32>(Q, src, dst, row0, nrows, g, st);
+        case ST_FP16S: return dec_q<ST_FP16S>(Q, src, dst, row0, nrows, g, st);
+        case ST_BF16S: return dec_q<ST_BF16S>(Q, src, dst, row0, nrows, g, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// ---- ghost layer (halo_thread in step_kernels.cuh) over the six faces ----
+template <int Q, typename W>
+__global__ void __launch_bounds__(128) k_halo(W* f, const uint8_t* __restrict__ flags, const uint16_t* __restrict__ bc,
+                                              PadGeom g, long long n)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= count) return;
-    const long long e = start + t;
-    const int q = (int)(e / E);
-    float w = 0.f;
-#pragma unroll
-    for (int p = 0; p < Q; p++)
-        if (p == q) w = lat_w(Q, p);
-    dst[t] = Codec<S>::load(src + e, w);
+    if (t < n) halo_thread<Q, W>(f, flags, bc, g, t);
 }
 
-template <int S>
-static cudaError_t enc_q(int Q, const float* src, void* dst, long long start, long long count, long long E, cudaStream_t st)
+cudaError_t halo_fill(int Q, int tsize, void* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
+                      cudaStream_t st)
 {
-    using T = typename Codec<S>::T;
-    const unsigned nb = (unsigned)((count + 255) / 256);
-    if (Q == 19) k_encode<S, 19><<<nb, 256, 0, st>>>(src, static_cast<T*>(dst), start, count, E);
-    else k_encode<S, 27><<<nb, 256, 0, st>>>(src, static_cast<T*>(dst), start, count, E);
-    return cudaGetLastError();
-}
-
-template <int S>
-static cudaError_t dec_q(int Q, const void* src, float* dst, long long start, long long count, long long E, cudaStream_t st)
-{
-    using T = typename Codec<S>::T;
-    const unsigned nb = (unsigned)((count + 255) / 256);
-    if (Q == 19) k_decode<S, 19><<<nb, 256, 0, st>>>(static_cast<const T*>(src), dst, start, count, E);
-    else k_decode<S, 27><<<nb, 256, 0, st>>>(static_cast<const T*>(src), dst, start, count, E);
-    return cudaGetLastError();
-}
-
-cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long start, long long count, long long E,
-                     cudaStream_t st)
-{
-    switch (storage) {
-        case ST_FP32: return cudaMemcpyAsync(static_cast<float*>(dst) + start, src, sizeof(float) * count,
-                                             cudaMemcpyDeviceToDevice, st);
-        case ST_FP16S: return enc_q<ST_FP16S>(Q, src, dst, start, count, E, st);
-        case ST_BF16S: return enc_q<ST_BF16S>(Q, src, dst, start, count, E, st);
+    const long long n = halo_threads(g);
+    const unsigned nb = (unsigned)((n + 127) / 128);
+    if (Q == 19) {
+        if (tsize == 4) k_halo<19, uint32_t><<<nb, 128, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g, n);
+        else k_halo<19, uint16_t><<<nb, 128, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g, n);
+    } else {
+        if (tsize == 4) k_halo<27, uint32_t><<<nb, 128, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g, n);
+        else k_halo<27, uint16_t><<<nb, 128, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g, n);
     }
-    return cudaErrorInvalidValue;
-}
-
-cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long start, long long count, long long E,
-                     cudaStream_t st)
-{
-    switch (storage) {
-        case ST_FP32: return cudaMemcpyAsync(dst, static_cast<const float*>(src) + start, sizeof(float) * count,
-                                             cudaMemcpyDeviceToDevice, st);
-        case ST_FP16S: return dec_q<ST_FP16S>(Q, src, dst, start, count, E, st);
-        case ST_BF16S: return dec_q<ST_BF16S>(Q, src, dst, start, count, E, st);
-    }
-    return cudaErrorInvalidValue;
+    return cudaGetLastError();
 }
 
 __global__ void k_fill(float* p, float v, long long n)
@@ -323,27 +362,30 @@ cudaError_t reduce_force(const uint32_t* cells, long long n, const float* fx, co
 }
 
 template <int S, int Q>
-__global__ void k_reduce_mass(const typename Codec<S>::T* f, const uint8_t* flags, long long E, double* partial)
+__global__ void k_reduce_mass(const typename Codec<S>::T* f, const uint8_t* flags, long long E, PadGeom g,
+                              double* partial)
 {
     __shared__ double sh[REDUCE_BS / 32];
     double acc = 0.0;
     for (long long ic = (long long)blockIdx.x * REDUCE_BS + threadIdx.x; ic < E; ic += (long long)gridDim.x * REDUCE_BS) {
         if (flags[ic] & FL_SOLID) continue;
+        const long long row = ic / g.nx;
+        const long long ip = g.porg + (row / g.ny) * g.pxy + (row % g.ny) * g.px + (ic - row * g.nx);
         float r = 0.f;
 #pragma unroll
-        for (int q = 0; q < Q; q++) r += Codec<S>::load(f + (long long)q * E + ic, lat_w(Q, q));
+        for (int q = 0; q < Q; q++) r += Codec<S>::load(f + (long long)q * g.pE + ip, lat_w(Q, q));
         acc += (double)r;
     }
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
-cudaError_t reduce_mass(int storage, int Q, const void* f, const uint8_t* flags, long long E, double* partial,
-                        int nblocks, cudaStream_t st)
+cudaError_t reduce_mass(int storage, int Q, const void* f, const uint8_t* flags, long long E, const PadGeom& g,
+                        double* partial, int nblocks, cudaStream_t st)
 {
 #define LBFFS_MASS(S)                                                                                                  \
-    (Q == 19 ? (k_reduce_mass<S, 19><<<nblocks, REDUCE_BS, 0, st>>>(static_cast<const Codec<S>::T*>(f), flags, E, partial), 0) \
-             : (k_reduce_mass<S, 27><<<nblocks, REDUCE_BS, 0, st>>>(static_cast<const Codec<S>::T*>(f), flags, E, partial), 0))
+    (Q == 19 ? (k_reduce_mass<S, 19><<<nblocks, REDUCE_BS, 0, st>>>(static_cast<const Codec<S>::T*>(f), flags, E, g, partial), 0) \
+             : (k_reduce_mass<S, 27><<<nblocks, REDUCE_BS, 0, st>>>(static_cast<const Codec<S>::T*>(f), flags, E, g, partial), 0))
     switch (storage) {
         case ST_FP32: LBFFS_MASS(ST_FP32); break;
         case ST_FP16S: LBFFS_MASS(ST_FP16S); break;

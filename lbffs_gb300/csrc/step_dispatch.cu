@@ -3,26 +3,54 @@
 
 namespace lbffs {
 
-#define LBFFS_DECL(Q, S)                                                                                 \
-    cudaError_t launch_bulk_q##Q##_s##S##_inst(const StepArgs&, const StepConfig&, cudaStream_t);      \
-    cudaError_t launch_special_q##Q##_s##S##_inst(const StepArgs&, const StepConfig&, cudaStream_t);
-LBFFS_DECL(19, 0)
-LBFFS_DECL(19, 1)
-LBFFS_DECL(19, 2)
-LBFFS_DECL(27, 0)
-LBFFS_DECL(27, 1)
-LBFFS_DECL(27, 2)
-#undef LBFFS_DECL
+#define LBFFS_DECL4(Q, S, C)                                                          \
+    cudaError_t launch_step_q##Q##_s##S##_c##C##_p0(const StepArgs&, cudaStream_t); \
+    cudaError_t launch_step_q##Q##_s##S##_c##C##_p1(const StepArgs&, cudaStream_t); \
+    cudaError_t launch_step_q##Q##_s##S##_c##C##_p2(const StepArgs&, cudaStream_t); \
+    cudaError_t launch_step_q##Q##_s##S##_c##C##_p3(const StepArgs&, cudaStream_t);
+LBFFS_DECL4(19, 0, 0)
+LBFFS_DECL4(19, 1, 0)
+LBFFS_DECL4(19, 2, 0)
+LBFFS_DECL4(27, 0, 0)
+LBFFS_DECL4(27, 1, 0)
+LBFFS_DECL4(27, 2, 0)
+LBFFS_DECL4(27, 0, 1)
+LBFFS_DECL4(27, 1, 1)
+LBFFS_DECL4(27, 2, 1)
+#undef LBFFS_DECL4
 
-#define LBFFS_PICK(Q)                                                                                    \
-    switch (c.storage) {                                                                                 \
-        case ST_FP32: return bulk ? launch_bulk_q##Q##_s0_inst(a, c, st) : launch_special_q##Q##_s0_inst(a, c, st); \
-        case ST_FP16S: return bulk ? launch_bulk_q##Q##_s1_inst(a, c, st) : launch_special_q##Q##_s1_inst(a, c, st); \
-        case ST_BF16S: return bulk ? launch_bulk_q##Q##_s2_inst(a, c, st) : launch_special_q##Q##_s2_inst(a, c, st); \
-    }                                                                                                    \
-    return cudaErrorInvalidValue;
+typedef cudaError_t (*StepFn)(const StepArgs&, cudaStream_t);
 
-cudaError_t launch_q19(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st) { LBFFS_PICK(19) }
-cudaError_t launch_q27(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st) { LBFFS_PICK(27) }
+#define LBFFS_ROW(Q, S, C)                                                                                   \
+    {                                                                                                        \
+        launch_step_q##Q##_s##S##_c##C##_p0, launch_step_q##Q##_s##S##_c##C##_p1,                            \
+            launch_step_q##Q##_s##S##_c##C##_p2, launch_step_q##Q##_s##S##_c##C##_p3                         \
+    }
+
+// [storage][part]
+static const StepFn k19[3][4] = {LBFFS_ROW(19, 0, 0), LBFFS_ROW(19, 1, 0), LBFFS_ROW(19, 2, 0)};
+// [collision][storage][part]
+static const StepFn k27[2][3][4] = {{LBFFS_ROW(27, 0, 0), LBFFS_ROW(27, 1, 0), LBFFS_ROW(27, 2, 0)},
+                                    {LBFFS_ROW(27, 0, 1), LBFFS_ROW(27, 1, 1), LBFFS_ROW(27, 2, 1)}};
+#undef LBFFS_ROW
+
+static int part_of(const StepConfig& c, bool bulk)
+{
+    if (!bulk) return 3;
+    if (c.sgs == SGS_WALE) return 2;
+    return c.les ? 1 : 0;
+}
+
+cudaError_t launch_q19(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st)
+{
+    if (c.storage < 0 || c.storage > 2) return cudaErrorInvalidValue;
+    return k19[c.storage][part_of(c, bulk)](a, st);
+}
+
+cudaError_t launch_q27(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st)
+{
+    if (c.storage < 0 || c.storage > 2 || c.collision < 0 || c.collision > 1) return cudaErrorInvalidValue;
+    return k27[c.collision][c.storage][part_of(c, bulk)](a, st);
+}
 
 }  // namespace lbffs

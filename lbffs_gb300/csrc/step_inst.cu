@@ -1,49 +1,37 @@
-// One instantiation unit of the fused step kernels.  The build compiles this file once
-// per (lattice LBFFS_Q, storage LBFFS_S, part LBFFS_PART) so the heavy template
-// instantiations compile in parallel; step_dispatch.cu selects among them at run time.
+// One instantiation unit of the fused step kernels.  The build compiles this file once per
+// (lattice LBFFS_Q, storage LBFFS_S, collision LBFFS_C, part LBFFS_PART) so every heavy template
+// instantiation compiles in parallel; step_dispatch.cu selects among them at run time.
+//   LBFFS_PART 0: k_bulk, Smagorinsky with LES off;  1: k_bulk, Smagorinsky with LES on;
+//              2: k_bulk, WALE;                      3: k_special
 #include "launch.h"
 #include "step_kernels.cuh"
 
-#ifndef LBFFS_Q
-#error "LBFFS_Q, LBFFS_S and LBFFS_PART must be defined by the build"
+#if !defined(LBFFS_Q) || !defined(LBFFS_S) || !defined(LBFFS_C) || !defined(LBFFS_PART)
+#error "LBFFS_Q, LBFFS_S, LBFFS_C and LBFFS_PART must be defined by the build"
 #endif
 
-#define LBFFS_CAT2(a, b, c, d) launch_##a##_q##b##_s##c##_##d
-#define LBFFS_CAT(a, b, c, d) LBFFS_CAT2(a, b, c, d)
+#define LBFFS_NAME2(q, s, c, p) launch_step_q##q##_s##s##_c##c##_p##p
+#define LBFFS_NAME(q, s, c, p) LBFFS_NAME2(q, s, c, p)
 
 namespace lbffs {
 
-#if LBFFS_PART == 0
-template <int COLL>
-static void bulk_c(const StepArgs& a, const StepConfig& c, cudaStream_t st)
+cudaError_t LBFFS_NAME(LBFFS_Q, LBFFS_S, LBFFS_C, LBFFS_PART)(const StepArgs& a, cudaStream_t st)
 {
-    const dim3 grid((a.nx + BULK_BX - 1) / BULK_BX, a.ny, a.nz);
-    if (c.sgs == SGS_WALE) k_bulk<LBFFS_Q, LBFFS_S, COLL, SGS_WALE, false><<<grid, BULK_BX, 0, st>>>(a);
-    else if (c.les) k_bulk<LBFFS_Q, LBFFS_S, COLL, SGS_SMAG, true><<<grid, BULK_BX, 0, st>>>(a);
-    else k_bulk<LBFFS_Q, LBFFS_S, COLL, SGS_SMAG, false><<<grid, BULK_BX, 0, st>>>(a);
-}
-
-cudaError_t LBFFS_CAT(bulk, LBFFS_Q, LBFFS_S, inst)(const StepArgs& a, const StepConfig& c, cudaStream_t st)
-{
-#if LBFFS_Q == 27
-    if (c.collision == COLL_CUMULANT) bulk_c<COLL_CUMULANT>(a, c, st);
-    else
-#endif
-        bulk_c<COLL_RR>(a, c, st);
-    return cudaGetLastError();
-}
-#else
-cudaError_t LBFFS_CAT(special, LBFFS_Q, LBFFS_S, inst)(const StepArgs& a, const StepConfig& c, cudaStream_t st)
-{
+#if LBFFS_PART == 3
     if (a.n_special <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((a.n_special + SPECIAL_BS - 1) / SPECIAL_BS));
-#if LBFFS_Q == 27
-    if (c.collision == COLL_CUMULANT) k_special<LBFFS_Q, LBFFS_S, COLL_CUMULANT><<<grid, SPECIAL_BS, 0, st>>>(a);
-    else
+    k_special<LBFFS_Q, LBFFS_S, LBFFS_C><<<grid, SPECIAL_BS, 0, st>>>(a);
+#else
+    const dim3 grid((a.nx + BULK_BX * BULK_V - 1) / (BULK_BX * BULK_V), a.ny, a.nz);
+#if LBFFS_PART == 0
+    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_SMAG, false><<<grid, BULK_BX, 0, st>>>(a);
+#elif LBFFS_PART == 1
+    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_SMAG, true><<<grid, BULK_BX, 0, st>>>(a);
+#else
+    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_WALE, false><<<grid, BULK_BX, 0, st>>>(a);
 #endif
-        k_special<LBFFS_Q, LBFFS_S, COLL_RR><<<grid, SPECIAL_BS, 0, st>>>(a);
+#endif
     return cudaGetLastError();
 }
-#endif
 
 }  // namespace lbffs

@@ -16,12 +16,13 @@
 // Both kernels read only the previous-step populations and previous-step macroscopic
 // buffers and write disjoint cells, so they need no ordering between them.
 #pragma once
+#include <type_traits>
+
 #include "collide.cuh"
 #include "lbffs_common.cuh"
 
 namespace lbffs {
 
-constexpr int BULK_BX = 128;
 constexpr int SPECIAL_BS = 128;
 
 template <int Q>
@@ -198,126 +199,30 @@ __device__ __forceinline__ int missing_dir(int q, const int (&b)[3])
     return out;
 }
 
-// Face-aware pull for the bulk kernel: per axis, the index correction of a periodic wrap and the
-// "missing link" flag of a wall are computed once per cell; each direction then only adds the
-// corrections of its nonzero components (the selection is resolved at compile time).
-struct FaceAxes {
-    long long wlo[3], whi[3];  // index correction when pulling across the low / high face (wrap)
-    bool mlo[3], mhi[3];       // pulling across the low / high face hits a wall (bounce-back / mirror)
-    bool sym[3];               // Symmetry code on that axis
-};
-
-__device__ __forceinline__ FaceAxes face_axes(const int (&x)[3], const int (&N)[3], const long long (&st)[3],
-                                              uint16_t bw)
-{
-    FaceAxes fa;
-    const bool face = (bw >> 9) & 1;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const int b = (bw >> (3 * d)) & 7;
-        const bool wall = face && is_wall_code(b);
-        fa.wlo[d] = (x[d] == 0) ? (long long)N[d] * st[d] : 0;
-        fa.whi[d] = (x[d] == N[d] - 1) ? -(long long)N[d] * st[d] : 0;
-        fa.mlo[d] = (x[d] == 0) && wall;
-        fa.mhi[d] = (x[d] == N[d] - 1) && wall;
-        fa.sym[d] = b == BC_SYM;
-    }
-    return fa;
-}
-
-template <int Q>
-__device__ __forceinline__ int missing_dir_sym(int q, const bool (&sym)[3])
-{
-    const int c0 = lat_c(Q, q, 0), c1 = lat_c(Q, q, 1), c2 = lat_c(Q, q, 2);
-    const int r = lat_opp(Q, q);
-    if (Q == 19) {
-        if ((c0 != 0) + (c1 != 0) + (c2 != 0) < 2) return r;
-        const int fa = c0 ? lat_find(Q, -c0, c1, c2) : lat_find(Q, c0, -c1, c2);  // first nonzero axis
-        const int fb = c2 ? lat_find(Q, c0, c1, -c2) : lat_find(Q, c0, -c1, c2);  // second nonzero axis
-        const bool sa = c0 ? sym[0] : sym[1];
-        const bool sb = c2 ? sym[2] : sym[1];
-        return sa ? fa : (sb ? fb : r);
-    }
-    int out = r;
-    if (sym[0]) out = c0 ? lat_find(Q, -c0, c1, c2) : r;
-    if (sym[1]) out = c1 ? lat_find(Q, c0, -c1, c2) : r;
-    if (sym[2]) out = c2 ? lat_find(Q, c0, c1, -c2) : r;
-    return out;
-}
-
-// plane and cell that population q of cell ic is pulled from
-template <int Q>
-__device__ __forceinline__ int pull_src(int q, long long ic, const long long (&st)[3], const FaceAxes& fa, int& plane)
-{
-    long long idx = ic;
-    bool miss = false;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const int c = lat_c(Q, q, d);
-        if (c == 1) {
-            idx += fa.wlo[d] - st[d];
-            miss |= fa.mlo[d];
-        } else if (c == -1) {
-            idx += fa.whi[d] + st[d];
-            miss |= fa.mhi[d];
-        }
-    }
-    plane = miss ? missing_dir_sym<Q>(q, fa.sym) : q;
-    return miss ? (int)ic : (int)idx;
-}
-
-// ------------------------------------------------------------------------------------------
+// The bulk step of one fluid cell whose Q populations are already in ft (held form for D3Q19):
+// macroscopics, eddy viscosity, sponge, collision, and the Q streaming stores at ip.
 template <int Q, int S, int COLL, int SGS, bool LES>
-__global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
+__device__ __forceinline__ void bulk_cell(const StepArgs& a, float (&ft)[Q], uint8_t fl, int i, int j, int k, int ic,
+                                          int ip)
 {
     using T = typename Codec<S>::T;
-    const int i = blockIdx.x * BULK_BX + threadIdx.x;
-    if (i >= a.nx) return;
-    const int j = blockIdx.y, k = blockIdx.z;
-    const long long ic = ((long long)k * a.ny + j) * a.nx + i;
-    const uint8_t fl = __ldg(a.flags + ic);
-    if (fl & (FL_SOLID | FL_SPECIAL)) return;
-
-    const T* fin = static_cast<const T*>(a.f_in);
-    T* fout = static_cast<T*>(a.f_out);
-    // D3Q19 holds f (FP32 storage) or f - w (shifted storage) through the whole step; D3Q27 holds f
     constexpr bool HELD = (Q == 19);
-    auto ld = [&](int plane, int cell, int q) {
-        const T* p = static_cast<const T*>(a.fin_q[plane]) + cell;
-        return HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
-    };
-    const int ic32 = (int)ic;
-    float ft[Q];
-    if (__any_sync(__activemask(), (fl & FL_FACE) != 0)) {
-        // a warp with a domain-face cell (walls, periodic wrap, symmetry only: upwindID_B with
-        // bounce-back or mirror, kernel.cl:328-575 / 114-326); interior lanes get zero corrections
-        const long long st[3] = {1, a.nx, (a.nz > 1) ? (long long)a.nx * a.ny : 0};
-        const int x[3] = {i, j, k}, N[3] = {a.nx, a.ny, a.nz};
-        const FaceAxes fa = face_axes(x, N, st, __ldg(a.bc + ic));
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            int plane;
-            const int cell = pull_src<Q>(q, ic, st, fa, plane);
-            ft[q] = ld(plane, cell, q);
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < Q; q++) ft[q] = ld(q, ic32 - a.pull_off[q], q);
-    }
     const float omega = (fl & FL_OMEGA) ? __ldg(a.omega + ic) : a.omega0;
     float rho, u, v, w, tsgs = 0.f;
     if constexpr (Q == 19) {
-        const Mom19 m = moments19<Codec<S>::DEV>(ft);
+        constexpr int HS = Codec<S>::HS;
+        const Mom19 m = moments19<Codec<S>::DEV, HS>(ft);
         rho = m.rho;
         const float ir = 1.f / rho;
-        u = m.j[0] * ir + 0.5f * a.dpdx * ir;  // updateRhoUVW (kernel.cl:3509-3523)
-        v = m.j[1] * ir;
-        w = m.j[2] * ir;
+        const float irs = ir * (1.f / HS);
+        u = m.j[0] * irs + 0.5f * a.dpdx * ir;  // updateRhoUVW (kernel.cl:3509-3523)
+        v = m.j[1] * irs;
+        w = m.j[2] * irs;
         if constexpr (SGS == SGS_WALE) {
             const float own[3] = {u, v, w};
             tsgs = wale_general(a, i, j, k, ic, own);
         } else if constexpr (LES) {
-            tsgs = smagorinsky19(m, u, v, w, omega, a.les, a.cs);
+            tsgs = smagorinsky19<HS>(m, u, v, w, omega, a.les, a.cs);
             if (fl & FL_SDF) tsgs = damping(tsgs, __ldg(a.sdf + ic), a.cs);
         }
         if (a.err && !(rho == rho)) atomicOr(a.err, 1);
@@ -331,7 +236,7 @@ __global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
             a.tau_n[ic] = tsgs;
         }
         const float U[3] = {u - 0.5f * a.dpdx * ir, v, w};
-        collide_rr19m(ft, m, U, we, a.omega_b, a.dpdx);
+        collide_rr19m<HS>(ft, m, U, we, a.omega_b, a.dpdx);
     } else {
         macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
         if constexpr (SGS == SGS_WALE) {
@@ -353,20 +258,70 @@ __global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
         }
         collide<Q, COLL>(ft, rho, u, v, w, we, a);
     }
+    char* pout = a.fout_base + (long long)ip * (long long)sizeof(T);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-        T* p = static_cast<T*>(a.fout_q[q]) + ic32;
+        T* p = reinterpret_cast<T*>(pout + a.plane_b[q]);
         if constexpr (HELD) Codec<S>::store_held(p, ft[q]);
         else Codec<S>::store(p, ft[q], lat_w(Q, q));
     }
 }
 
-template <int Q, int S, int COLL>
-__global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
+// One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
+// instruction of a warp covers 32 consecutive cells.  Every population is pulled from the same
+// offset for every cell: cells on the domain border read the ghost layer, which k_halo filled
+// with the reference's face streaming at the start of the step.
+// One CTA tile: BULK_BX * BULK_V cells of row (j, k) starting at x-block xb.
+template <int Q, int S, int COLL, int SGS, bool LES>
+__device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int k)
 {
     using T = typename Codec<S>::T;
-    const long long t = (long long)blockIdx.x * SPECIAL_BS + threadIdx.x;
-    if (t >= a.n_special) return;
+    constexpr bool HELD = (Q == 19);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i0 = (xb * (BULK_BX / 32) + warp) * (32 * BULK_V) + lane;
+    const int row = (k * a.ny + j) * a.nx;
+    const int prow = pidx(a, 0, j, k);
+    uint8_t fl[BULK_V];
+    bool act[BULK_V];
+    bool any = false;
+#pragma unroll
+    for (int v = 0; v < BULK_V; v++) {
+        const int i = i0 + 32 * v;
+        fl[v] = (i < a.nx) ? __ldg(a.flags + row + i) : FL_SOLID;
+        act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
+        any |= act[v];
+    }
+    if (!any) return;
+    float ft[BULK_V][Q];
+#pragma unroll
+    for (int v = 0; v < BULK_V; v++) {
+        if (!act[v]) continue;
+        const char* pin = a.fin_base + (long long)(prow + i0 + 32 * v) * (long long)sizeof(T);
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const T* p = reinterpret_cast<const T*>(pin + a.pull_b[q]);
+            ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < BULK_V; v++) {
+        if (!act[v]) continue;
+        const int i = i0 + 32 * v;
+        bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], i, j, k, row + i, prow + i);
+    }
+}
+
+template <int Q, int S, int COLL, int SGS, bool LES>
+__global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
+{
+    bulk_block<Q, S, COLL, SGS, LES>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// The general boundary path of entry t of the special list.
+template <int Q, int S, int COLL>
+__device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
+{
+    using T = typename Codec<S>::T;
     const long long ic = a.special[t];
     const int N[3] = {a.nx, a.ny, a.nz};
     const long long nxny = (long long)a.nx * a.ny;
@@ -378,20 +333,25 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
         y[d] = side < 0 ? min(1, N[d] - 1) : max(N[d] - 2, 0);
         return id(y[0], y[1], y[2]);
     };
+    auto inner_p = [&](int d, int side) {
+        int y[3] = {x[0], x[1], x[2]};
+        y[d] = side < 0 ? min(1, N[d] - 1) : max(N[d] - 2, 0);
+        return pidx(a, y[0], y[1], y[2]);
+    };
+    const int ip = pidx(a, x[0], x[1], x[2]);
     const uint16_t bw = a.bc[ic];
     const int b[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
     const bool face = (bw >> 9) & 1;
-    const T* fin = static_cast<const T*>(a.f_in);
-    T* fout = static_cast<T*>(a.f_out);
-    const long long E = a.E;
-    auto F = [&](int q, long long cell) { return Codec<S>::load(fin + (long long)q * E + cell, lat_w(Q, q)); };
+    // population q of the padded cell pcell (previous step)
+    auto F = [&](int q, int pcell) {
+        return Codec<S>::load(static_cast<const T*>(a.fin_q[q]) + pcell, lat_w(Q, q));
+    };
 
+    // streaming: upwind value, or the ghost that holds the face rule's value (upwindID_B +
+    // reflectOrMirrorQ, filled by k_halo)
     float ft[Q];
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-        const long long up = (q == 0) ? ic : upwind<Q>(q, x, N, b, face);
-        ft[q] = (up >= 0) ? F(q, up) : F(missing_dir<Q>(q, b), ic);
-    }
+    for (int q = 0; q < Q; q++) ft[q] = Codec<S>::load(static_cast<const T*>(a.fin_s[q]) + ip, lat_w(Q, q));
 
     const float uo[3] = {a.u_p[ic], a.v_p[ic], a.w_p[ic]};
     if (face) {
@@ -457,12 +417,12 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
 #pragma unroll
                 for (int side = -1; side <= 1; side += 2) {
                     if (!((side < 0 && x[d] == 0) || (side > 0 && x[d] == N[d] - 1))) continue;
-                    const long long in = inner(d, side);
+                    const int in = inner_p(d, side);
                     const float g = cs - uo[d];
 #pragma unroll
                     for (int q = 1; q < Q; q++) {
                         if (lat_c(Q, q, d) != -side) continue;
-                        ft[q] = g * F(q, in) + (1.f - g) * F(q, ic);
+                        ft[q] = g * F(q, in) + (1.f - g) * F(q, ip);
                     }
                 }
             }
@@ -480,7 +440,7 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
             const long long up = upwind<Q>(q, x, N, b, face);
             if (up < 0 || a.solid[up] != 1) continue;
             const int qb = lat_opp(Q, q);
-            const float fb = F(qb, ic);
+            const float fb = F(qb, ip);
             if (a.wall == WALL_BB) {
                 ft[q] = fb;
             } else {
@@ -545,7 +505,159 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
         collide<Q, COLL>(ft, rho, u, v, w, 1.f / (tau + tsgs), a);
     }
 #pragma unroll
-    for (int q = 0; q < Q; q++) Codec<S>::store(fout + (long long)q * E + ic, ft[q], lat_w(Q, q));
+    for (int q = 0; q < Q; q++) Codec<S>::store(static_cast<T*>(a.fout_q[q]) + ip, ft[q], lat_w(Q, q));
+}
+
+template <int Q, int S, int COLL>
+__global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
+{
+    const long long t = (long long)blockIdx.x * SPECIAL_BS + threadIdx.x;
+    if (t < a.n_special) special_cell<Q, S, COLL>(a, t);
+}
+
+// missing_dir for a direction q known at compile time: every lattice lookup is a constant
+template <int Q, int q>
+__device__ __forceinline__ int missing_dir_ct(const int (&b)[3])
+{
+    constexpr int c0 = lat_c(Q, q, 0), c1 = lat_c(Q, q, 1), c2 = lat_c(Q, q, 2);
+    constexpr int r = lat_opp(Q, q);
+    constexpr int mx = c0 ? lat_find(Q, -c0, c1, c2) : r;
+    constexpr int my = c1 ? lat_find(Q, c0, -c1, c2) : r;
+    constexpr int mz = c2 ? lat_find(Q, c0, c1, -c2) : r;
+    if constexpr (Q == 19) {
+        if constexpr ((c0 != 0) + (c1 != 0) + (c2 != 0) < 2) {
+            return r;
+        } else {
+            if (c0 != 0 && b[0] == BC_SYM) return mx;  // first Symmetry axis among the nonzero components
+            if (c1 != 0 && b[1] == BC_SYM) return my;
+            if (c2 != 0 && b[2] == BC_SYM) return mz;
+            return r;
+        }
+    } else {
+        int out = r;  // the last Symmetry axis wins; a zero component falls back to reflection
+        if (b[0] == BC_SYM) out = mx;
+        if (b[1] == BC_SYM) out = my;
+        if (b[2] == BC_SYM) out = mz;
+        return out;
+    }
+}
+
+// ---- ghost layer: the reference's face streaming for populations that cross the grid edge ----
+// Every population q of a cell P whose upwind neighbour P - c_q lies outside the grid is pulled
+// from the ghost P - c_q.  The ghost holds the value upwindID_B / reflectOrMirrorQ would pull
+// (D3Q19 kernel.cl:114-575, D3Q27 kernel.cl:1133-1146): the periodically wrapped upwind cell's
+// value, or, when a crossed face of P carries a wall code, P's own value of the bounce-back /
+// mirror direction.  The fill runs over the six faces of the grid: one thread per cell of a face
+// handles the directions that cross that face outward-in (5 for D3Q19, 9 for D3Q27), gathering
+// all of them before writing.  A diagonal crossing two faces at an edge is handled by both face
+// threads with the same value.  Raw element copies (W: the element's bit pattern): no rounding.
+// compile-time loop: f(std::integral_constant<int, I>) for I in [I0, N)
+template <int I0, int N, class F>
+__device__ __forceinline__ void static_for(F&& f)
+{
+    if constexpr (I0 < N) {
+        f(std::integral_constant<int, I0>{});
+        static_for<I0 + 1, N>(f);
+    }
+}
+
+template <int Q, int AXIS, int SIGN>
+__host__ __device__ constexpr int side_dir(int n)
+{
+    // the n-th direction q with c_q[AXIS] == SIGN
+    for (int q = 1, m = 0; q < Q; q++)
+        if (lat_c(Q, q, AXIS) == SIGN) {
+            if (m == n) return q;
+            m++;
+        }
+    return -1;
+}
+
+template <int Q>
+__host__ __device__ constexpr int side_count()
+{
+    return Q == 19 ? 5 : 9;
+}
+
+// Face thread: cell x on the face AXIS = (SIGN > 0 ? 0 : N - 1), which pulls across that face the
+// directions with c[AXIS] == SIGN.
+template <int Q, typename W, int AXIS, int SIGN>
+__device__ __forceinline__ void halo_face_cell(W* f, const uint8_t* __restrict__ flags, const uint16_t* __restrict__ bc,
+                                               const int (&x)[3], const PadGeom& g)
+{
+    const int N[3] = {g.nx, g.ny, g.nz};
+    const long long ic = ((long long)x[2] * g.ny + x[1]) * g.nx + x[0];
+    if (__ldg(flags + ic) & FL_SOLID) return;  // nobody pulls through a solid cell's ghosts
+    const uint16_t bw = __ldg(bc + ic);
+    const int b[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
+    const bool face = (bw >> 9) & 1;
+    const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
+    constexpr int NQ = side_count<Q>();
+    W v[NQ];
+    static_for<0, NQ>([&](auto n) {
+        constexpr int q = side_dir<Q, AXIS, SIGN>(decltype(n)::value);
+        int up[3];
+        bool miss = false;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            up[d] = x[d] - lat_c(Q, q, d);
+            if (up[d] < 0) {
+                miss |= face && is_wall_code(b[d]);
+                up[d] += N[d];
+            } else if (up[d] >= N[d]) {
+                miss |= face && is_wall_code(b[d]);
+                up[d] -= N[d];
+            }
+        }
+        v[decltype(n)::value] = miss ? __ldg(f + (long long)missing_dir_ct<Q, q>(b) * g.pE + ip)
+                                     : __ldg(f + (long long)q * g.pE + g.porg + up[2] * g.pxy + up[1] * g.px + up[0]);
+    });
+    static_for<0, NQ>([&](auto n) {
+        constexpr int q = side_dir<Q, AXIS, SIGN>(decltype(n)::value);
+        constexpr int cx = lat_c(Q, q, 0), cy = lat_c(Q, q, 1), cz = lat_c(Q, q, 2);
+        f[(long long)q * g.pE + ip - (cx + cy * g.px + cz * g.pxy)] = v[decltype(n)::value];
+    });
+}
+
+// Thread t of the ghost fill of one lattice (t < halo_threads(g)): faces in the order x-, x+,
+// y-, y+, z-, z+, each face a plane of cells in its own row-major order.
+template <int Q, typename W>
+__device__ __forceinline__ void halo_thread(W* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
+                                            long long t)
+{
+    const long long ax = (long long)g.ny * g.nz, ay = (long long)g.nx * g.nz, az = (long long)g.nx * g.ny;
+    int x[3];
+    if (t < 2 * ax) {
+        const bool hi = t >= ax;
+        const long long p = hi ? t - ax : t;
+        x[0] = hi ? g.nx - 1 : 0;
+        x[1] = (int)(p % g.ny);
+        x[2] = (int)(p / g.ny);
+        if (hi) halo_face_cell<Q, W, 0, -1>(f, flags, bc, x, g);
+        else halo_face_cell<Q, W, 0, 1>(f, flags, bc, x, g);
+        return;
+    }
+    t -= 2 * ax;
+    if (t < 2 * ay) {
+        const bool hi = t >= ay;
+        const long long p = hi ? t - ay : t;
+        x[0] = (int)(p % g.nx);
+        x[1] = hi ? g.ny - 1 : 0;
+        x[2] = (int)(p / g.nx);
+        if (hi) halo_face_cell<Q, W, 1, -1>(f, flags, bc, x, g);
+        else halo_face_cell<Q, W, 1, 1>(f, flags, bc, x, g);
+        return;
+    }
+    t -= 2 * ay;
+    if (t < 2 * az) {
+        const bool hi = t >= az;
+        const long long p = hi ? t - az : t;
+        x[0] = (int)(p % g.nx);
+        x[1] = (int)(p / g.nx);
+        x[2] = hi ? g.nz - 1 : 0;
+        if (hi) halo_face_cell<Q, W, 2, -1>(f, flags, bc, x, g);
+        else halo_face_cell<Q, W, 2, 1>(f, flags, bc, x, g);
+    }
 }
 
 }  // namespace lbffs
