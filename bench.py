@@ -119,6 +119,19 @@ def make_workload(name):
         solid, sdf = G.cylinder_z(1024, 256, 4, 256.0, cy, 20.0)
         c = K.make_case(1024, 256, 4, 19, K.channel_faces(0.05), nu=0.02, solid=solid, sdf=sdf)
         return c, dict(collision="rr", sgs="smag", wall="ibb", les=0.0)
+    if name == "step768_q27":
+        # backward-facing step: 768x192x192, step 64 high ending at x = 128, inlet 0.06 with a
+        # seeded +-1 % per-cell perturbation, Re 5500 on the step height, Smagorinsky LES with the
+        # near-wall damping, sponge over the last 64 cells before the Geier outlet
+        nx, ny, nz, h = 768, 192, 192, 64
+        solid, sdf = G.backward_step(nx, ny, nz, 128, h)
+        c = K.make_case(nx, ny, nz, 27, K.channel_faces(0.06, top_bottom=K.BOUNCEBACK, z_periodic=True),
+                        nu=0.06 * h / 5500.0, solid=solid, sdf=sdf)
+        rng = np.random.default_rng(3)
+        inlet = c.boundary1 == K.FIXEDVELOCITY
+        c.u0[inlet] *= (1.0 + rng.uniform(-0.01, 0.01, int(inlet.sum()))).astype(np.float32)
+        c.f = None
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=64.0 / nx, rest=True)
     raise KeyError(name)
 
 
@@ -243,7 +256,12 @@ def describe(name, storage):
     return {"cavity256": f"lid-driven cavity D3Q19 RR {storage.upper()} 256^3, nu=0.032, lid 0.05 (synthetic)",
             "cavity128": f"lid-driven cavity D3Q19 RR {storage.upper()} 128^3 (synthetic, profiling size)",
             "cavity256_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256^3 (synthetic)",
-            "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)"}[name]
+            "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)",
+            "step768_q27": f"backward-facing step D3Q27 RR IBB LES {storage.upper()} 768x192x192, step 64, Re 5500, "
+                           "sponge 64 cells (synthetic)"}[name]
+
+
+BULK_KIND = 0  # D3Q19 bulk kernel variant (--bulk-kind)
 
 
 def run_device(name, storage, steps, warmup, device, timing_pass=True):
@@ -252,9 +270,18 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
     c, sel = make_workload(name)
     lat = L.Lattice(c.nx, c.ny, c.nz, q=c.q, storage=storage, collision=sel["collision"], sgs=sel["sgs"],
                     wall=sel["wall"], device=device)
-    lat.load_case(c)
+    if c.q == 19:
+        lat.set_bulk_kernel(BULK_KIND)
+    if sel.get("rest"):
+        for name in ("boundary", "boundary1", "boundary2", "boundary3", "u0", "v0", "w0", "solid", "nei_solid", "sdf",
+                     "omega"):
+            lat.upload(name, getattr(c, name))
+        lat.init_rest()
+    else:
+        lat.load_case(c)
+    spz = sel.get("spz", 0.1)
     stream = torch.cuda.ExternalStream(lat.stream(), device=device)
-    lat.step(warmup, les=sel["les"], store_fields=0)
+    lat.step(warmup, les=sel["les"], spz_width=spz, store_fields=0)
     lat.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -262,7 +289,7 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
         torch.distributed.barrier()
     torch.cuda.synchronize(device)
     e0.record(stream)
-    lat.step(steps, les=sel["les"], store_fields=0)
+    lat.step(steps, les=sel["les"], spz_width=spz, store_fields=0)
     e1.record(stream)
     e1.synchronize()
     lat.synchronize()
@@ -274,7 +301,7 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
            "launches_per_step": 3 if counts["special"] > 0 else 2, "lat": lat, "case": c, "sel": sel}
     if timing_pass:
         lat.set_timing(True)
-        lat.step(steps, les=sel["les"], store_fields=0)
+        lat.step(steps, les=sel["les"], spz_width=spz, store_fields=0)
         bulk_ms, n = lat.kernel_time("bulk")
         sp_ms, nsp = lat.kernel_time("special")
         h_ms, nh = lat.kernel_time("halo")
@@ -360,10 +387,14 @@ def main():
     ap.add_argument("--requests", type=int, default=512, help="serving workload: number of requests")
     ap.add_argument("--step-scale", type=float, default=1.0, help="serving workload: step count scale")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--bulk-kind", type=int, default=0, choices=[0, 1],
+                    help="D3Q19 bulk kernel: 0 per-thread loads, 1 row-staged bulk copies")
     ap.add_argument("--profile", action="store_true",
                     help="device-timed steps only (no e2e, CPU baseline or variants): the command ncu captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    global BULK_KIND
+    BULK_KIND = args.bulk_kind
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -440,9 +471,11 @@ def main():
     variants = {}
     if rank == 0 and not args.no_variants and args.workload == "cavity256":
         for vname, vst in (("cavity256", "fp16s"), ("cavity256", "bf16s"), ("cavity256_q27", "fp32"),
-                           ("cavity256_q27", "fp16s"), ("cylinder1024", "fp32"), ("cylinder1024", "fp16s")):
+                           ("cavity256_q27", "fp16s"), ("cylinder1024", "fp32"), ("cylinder1024", "fp16s"),
+                           ("step768_q27", "fp32"), ("step768_q27", "fp16s")):
             try:
-                r = run_device(vname, vst, args.steps, args.warmup, device)
+                r = run_device(vname, vst, min(args.steps, 50) if vname == "step768_q27" else args.steps,
+                               args.warmup, device)
                 vq = r["case"].q
                 vb = BYTES_PER_CELL[(vq, vst)]
                 vn = r["fluid"] - r["special"]

@@ -169,6 +169,21 @@ int lbffs_kernel_time(lbffs_ctx* ctx, const char* name, double* total_ms, long l
 /* Counts of cells per class after the geometry commit: [fluid, special, link, store]. */
 int lbffs_cell_counts(lbffs_ctx* ctx, long long out[4]);
 
+/* No counterpart in the reference (a choice between two implementations of the same D3Q19 step,
+   which give identical results).  kind 0: each thread loads its cells' pulled populations from
+   HBM; kind 1: the pulled rows of a tile are staged in shared memory by bulk async copies and
+   clean tiles are written back the same way.  D3Q27 contexts always use kind 0. */
+int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
+
+/* setSolid + setNeiSolid (src/walls.hpp:159-216) on the device, bit for bit the reference's host
+   result: solid[ic] = 1 for cells inside the closed surface (ray-crossing parity of isInner,
+   walls.hpp:73-157, within the STL's bounding box, which the reference starts at the origin),
+   inverted when invert != 0 (invertFluidSolid); neiSolid from solid as setNeiSolid builds it.
+   vertices: ntri triangles x (v0, v1, v2) x (x, y, z) floats in lattice units, i.e. the STL's
+   vertices after normalizeSTLv (stl.hpp:161-175), all patches concatenated.  Replaces the SOLID
+   and NEISOLID fields; the geometry takes effect at the next lbffs_step. */
+int lbffs_voxelize(lbffs_ctx* ctx, const float* vertices, long long ntri, int invert);
+
 /* Set both population copies to the rest equilibrium rho = 1, u = 0 (f_q = w_q), the state
    initialization.hpp writes for a fluid at rest, without a host upload of F. */
 int lbffs_init_rest(lbffs_ctx* ctx);

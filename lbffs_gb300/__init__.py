@@ -92,6 +92,8 @@ def load_library():
         "lbffs_kernel_time": ([vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)], i),
         "lbffs_cell_counts": ([vp, C.POINTER(C.c_longlong)], i),
         "lbffs_init_rest": ([vp], i),
+        "lbffs_set_bulk_kernel": ([vp, i], i),
+        "lbffs_voxelize": ([vp, C.POINTER(C.c_float), C.c_longlong, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -170,6 +172,19 @@ class Lattice:
     def step(self, n=1, dpdx=0.0, les=0.0, omega_b=0.1, spz_width=0.1, clim=0.01, rho_av=1.0, store_fields=1):
         p = StepParams(dpdx, rho_av, les, omega_b, spz_width, clim, int(store_fields))
         self._check(self.lib.lbffs_step(self.h, C.byref(p), int(n)))
+
+    def voxelize(self, vertices, invert=False):
+        """setSolid + setNeiSolid of a closed triangle surface on the device (src/walls.hpp).
+
+        ``vertices``: (ntri, 3, 3) float32 in lattice units as the reference holds them after reading
+        the STL (stl.hpp normalizeSTLv)."""
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 9)
+        self._check(self.lib.lbffs_voxelize(self.h, v.ctypes.data_as(C.POINTER(C.c_float)), v.shape[0],
+                                            int(bool(invert))))
+
+    def set_bulk_kernel(self, kind):
+        """D3Q19 bulk kernel variant: 0 per-thread loads, 1 row-staged bulk copies (same results)."""
+        self._check(self.lib.lbffs_set_bulk_kernel(self.h, int(kind)))
 
     def init_rest(self):
         """Both population copies at rest (f_q = w_q) without a host upload."""

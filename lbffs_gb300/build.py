@@ -46,11 +46,12 @@ def build(verbose=False, extra_flags=None, jobs=None):
     hdrs = _headers()
     units = []  # (source, object, defines)
     for f in sorted(os.listdir(CSRC)):
-        if f.endswith((".cu", ".cpp")) and f not in ("step_inst.cu", "batch_inst.cu"):
+        if f.endswith((".cu", ".cpp")) and f not in ("step_inst.cu", "batch_inst.cu", "bulk_tma.cu"):
             units.append((f, os.path.splitext(f)[0] + ".o", []))
     # batched kernels of the server: one object per storage format
     for st in (0, 1, 2):
         units.append(("batch_inst.cu", f"batch_s{st}.o", [f"-DLBFFS_S={st}"]))
+        units.append(("bulk_tma.cu", f"bulk_tma_s{st}.o", [f"-DLBFFS_S={st}"]))
     # the step kernels: one object per (lattice, storage, collision, kernel variant) so they compile
     # in parallel (step_inst.cu lists the parts)
     for q, colls in ((19, (0,)), (27, (0, 1))):

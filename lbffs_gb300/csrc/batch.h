@@ -13,17 +13,22 @@ struct BatchCase {
     long long nsteps;  // steps the case runs in total
     int slot;          // index of the case's step counter
     int tiles_x;       // bulk tiles per row: ceil(nx / (BULK_BX * BULK_V))
+    int tiles;         // bulk tiles of the case
 };
 
-// Bulk step of every case in cases[0..ncases): CTA b runs tile b - tile_start[c] of the case c
-// with tile_start[c] <= b < tile_start[c + 1] (ntiles = tile_start[ncases]).
+// bulk tiles one CTA of the batched kernel runs (one case's argument copy serves them all)
+constexpr int BATCH_TILES_PER_CTA = 8;
+
+// Bulk step of every case in cases[0..ncases): CTA b runs run b - tile_start[c] of the case c
+// with tile_start[c] <= b < tile_start[c + 1] (prefix sums of runs of BATCH_TILES_PER_CTA tiles;
+// ntiles = tile_start[ncases] CTAs).
 cudaError_t batch_bulk(int storage, bool les, const BatchCase* cases, const int* tile_start, int ncases, int ntiles,
                        const long long* done, cudaStream_t st);
 // Boundary step: thread t runs entry t - sp_start[c] of case c's special list.
 cudaError_t batch_special(int storage, const BatchCase* cases, const long long* sp_start, int ncases,
                           long long nspecial, const long long* done, cudaStream_t st);
-// Ghost layers: thread t fills ghost thread t - h_start[c] of case c's source populations.
-cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nthreads,
+// Ghost layers: CTA b runs ghost-fill block b - h_start[c] of case c's source populations.
+cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nblocks,
                        const long long* done, cudaStream_t st);
 // Advance the step counters of the listed slots that have not reached their nsteps.
 cudaError_t batch_tick(const int* slots, const long long* nsteps, int n, long long* done, cudaStream_t st);

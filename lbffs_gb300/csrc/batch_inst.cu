@@ -50,10 +50,13 @@ __global__ void __launch_bounds__(BULK_BX) k_bulk_batch(const BatchCase* __restr
     __syncthreads();
     if (threadIdx.x == 0 && s_last) sa.store_all = 1;  // full macroscopic fields on the final step
     __syncthreads();
-    const int tile = (int)blockIdx.x - tile_start[s_case];
-    const int tx = cases[s_case].tiles_x;
-    const int xb = tile % tx, row = tile / tx;
-    bulk_block<19, S, COLL_RR, SGS_SMAG, LES>(sa, xb, row % sa.ny, row / sa.ny);
+    const int run = (int)blockIdx.x - tile_start[s_case];
+    const int tx = cases[s_case].tiles_x, tiles = cases[s_case].tiles;
+    const int t1 = min(tiles, (run + 1) * BATCH_TILES_PER_CTA);
+    for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++) {
+        const int xb = tile % tx, row = tile / tx;
+        bulk_block<19, S, COLL_RR, SGS_SMAG, LES>(sa, xb, row % sa.ny, row / sa.ny);
+    }
 }
 
 __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* __restrict__ cases,
@@ -70,19 +73,19 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* _
 
 using W = typename std::conditional<S == ST_FP32, uint32_t, uint16_t>::type;
 
-__global__ void __launch_bounds__(128) k_halo_batch(const BatchCase* __restrict__ cases,
-                                                    const long long* __restrict__ h_start, int ncases,
-                                                    const long long* __restrict__ done)
+// CTA b runs ghost-fill block b - h_start[c] of case c (h_start: prefix sums of halo blocks)
+__global__ void __launch_bounds__(HALO_BS) k_halo_batch(const BatchCase* __restrict__ cases,
+                                                        const long long* __restrict__ h_start, int ncases,
+                                                        const long long* __restrict__ done)
 {
-    const long long t = (long long)blockIdx.x * 128 + threadIdx.x;
-    if (t >= h_start[ncases]) return;
-    const int c = find_case<long long>(h_start, ncases, t);
+    const long long b = blockIdx.x;
+    const int c = find_case<long long>(h_start, ncases, b);
     const long long d = done[cases[c].slot];
     if (d >= cases[c].nsteps) return;
     const StepArgs& a = cases[c].args[d & 1];
     const PadGeom g{a.nx, a.ny, a.nz, a.px, a.pxy, a.porg, a.pE};
     // the ghosts of this step's source copy (k_bulk / k_special read it only after this launch)
-    halo_thread<19, W>(static_cast<W*>(const_cast<void*>(a.f_in)), a.flags, a.bc, g, t - h_start[c]);
+    halo_block<19, W>(static_cast<W*>(const_cast<void*>(a.f_in)), a.flags, a.bc, g, b - h_start[c], threadIdx.x);
 }
 
 }  // namespace
@@ -109,10 +112,10 @@ cudaError_t LBFFS_CAT(batch_special_s, LBFFS_S)(const BatchCase* cases, const lo
 }
 
 cudaError_t LBFFS_CAT(batch_halo_s, LBFFS_S)(const BatchCase* cases, const long long* h_start, int ncases,
-                                             long long nthreads, const long long* done, cudaStream_t st)
+                                             long long nblocks, const long long* done, cudaStream_t st)
 {
-    if (nthreads <= 0) return cudaSuccess;
-    k_halo_batch<<<(unsigned)((nthreads + 127) / 128), 128, 0, st>>>(cases, h_start, ncases, done);
+    if (nblocks <= 0) return cudaSuccess;
+    k_halo_batch<<<(unsigned)nblocks, HALO_BS, 0, st>>>(cases, h_start, ncases, done);
     return cudaGetLastError();
 }
 

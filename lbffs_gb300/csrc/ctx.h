@@ -59,6 +59,7 @@ struct lbffs_ctx {
 
     // timing
     bool timing = false;
+    int bulk_kind = 0;  // D3Q19 bulk kernel variant (lbffs_set_bulk_kernel)
     struct Ev {
         cudaEvent_t a, b;
         int kind;

@@ -16,6 +16,10 @@ struct StepConfig {
 
 // One half of a time step: bulk=true launches k_bulk, bulk=false launches k_special.
 cudaError_t launch_q19(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st);
+// row-staged D3Q19 bulk kernel (bulk_tma.cu, one object per storage format)
+cudaError_t launch_bulk_tma_s0(const StepArgs& a, int sgs, bool les, cudaStream_t st);
+cudaError_t launch_bulk_tma_s1(const StepArgs& a, int sgs, bool les, cudaStream_t st);
+cudaError_t launch_bulk_tma_s2(const StepArgs& a, int sgs, bool les, cudaStream_t st);
 cudaError_t launch_q27(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st);
 
 // setup.cu
@@ -42,6 +46,10 @@ cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long 
 cudaError_t halo_fill(int Q, int tsize, void* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
                       cudaStream_t st);
 cudaError_t fill_f32(float* p, float v, long long n, cudaStream_t st);
+// out[0] bit 0: a WallFunction code present, bit 1: an invalid code present (out[1]: the largest)
+cudaError_t setup_check_codes(const int* b1, const int* b2, const int* b3, long long E, int* out, cudaStream_t st);
+// counts[4] (zeroed by the caller): fluid, special, STL-link and macroscopic-storing cells
+cudaError_t setup_count_flags(const uint8_t* flags, long long E, unsigned long long* counts, cudaStream_t st);
 // FP64 partial sums: force over the listed cells (3 per block), mass over fluid cells (1 per block)
 constexpr int REDUCE_BS = 256;
 cudaError_t reduce_force(const uint32_t* cells, long long n, const float* fx, const float* fy, const float* fz,

@@ -1,6 +1,7 @@
 // C-ABI implementation (include/lbffs_cuda.h): context lifetime, field transfer,
 // geometry commit, the step loop and reductions.  Host code only; kernels live in
 // step_inst.cu / step_dispatch.cu, setup.cu and ibm.cu.
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -322,19 +323,22 @@ static int commit(lbffs_ctx* c)
 {
     const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
     const long long E = c->E;
-    // validate boundary codes (WallFunction, code 7, is not built)
-    std::vector<int> codes(E);
+    // validate boundary codes on the device (WallFunction, code 7, is not built)
+    {
+        int* chk = nullptr;
+        CK(ctx_alloc_bytes(c, (void**)&chk, 2 * sizeof(int)));
+        int init[2] = {0, INT_MIN}, res[2];
+        cudaError_t e = cudaMemcpyAsync(chk, init, sizeof(init), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = setup_check_codes(c->iarr[1], c->iarr[2], c->iarr[3], E, chk, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(res, chk, sizeof(res), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        ctx_free(c, chk);
+        CK(e);
+        if (res[0] & 1) return fail(c, LBFFS_E_UNSUPPORTED, "boundary code 7 (WallFunction) is not supported");
+        if (res[0] & 2) return fail(c, LBFFS_E_ARG, "invalid boundary code " + std::to_string(res[1]));
+    }
+    // sponge zone face-centre codes (tauSpongeZone, kernel.cl:2447-2501)
     for (int b = 1; b <= 3; b++) {
-        CK(cudaMemcpyAsync(codes.data(), c->iarr[b], sizeof(int) * E, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        for (long long i = 0; i < E; i++) {
-            const int v = codes[i];
-            if (v == BC_WALLFN)
-                return fail(c, LBFFS_E_UNSUPPORTED, "boundary code 7 (WallFunction) is not supported");
-            if (!(v == 0 || v == 1 || v == 3 || v == 4 || v == 5 || v == 6))
-                return fail(c, LBFFS_E_ARG, "invalid boundary code " + std::to_string(v));
-        }
-        // sponge zone face-centre codes (tauSpongeZone, kernel.cl:2447-2501)
         const long long cen[2] = {b == 1   ? ((long long)(nz / 2) * ny + ny / 2) * nx + 0
                                   : b == 2 ? ((long long)(nz / 2) * ny + 0) * nx + nx / 2
                                            : ((long long)0 * ny + ny / 2) * nx + nx / 2,
@@ -342,7 +346,9 @@ static int commit(lbffs_ctx* c)
                                   : b == 2 ? ((long long)(nz / 2) * ny + ny - 1) * nx + nx / 2
                                            : ((long long)(nz - 1) * ny + ny / 2) * nx + nx / 2};
         for (int s = 0; s < 2; s++) {
-            const int v = codes[cen[s]];
+            int v = 0;
+            CK(cudaMemcpyAsync(&v, c->iarr[b] + cen[s], sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
             const int bit = 2 * (b - 1) + s;
             if (v == BC_OUTLET || v == BC_FIXDEN) c->sponge_mask |= (1 << bit);
             else c->sponge_mask &= ~(1 << bit);
@@ -367,23 +373,19 @@ static int commit(lbffs_ctx* c)
         if (r != LBFFS_OK) return r;
     }
 
-    // per-class counts and zeroed link forces
-    std::vector<uint8_t> fl(E);
-    CK(cudaMemcpyAsync(fl.data(), c->flags, E, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    long long nf = 0, ns = 0, nl = 0, nst = 0;
-    for (long long i = 0; i < E; i++) {
-        const uint8_t v = fl[i];
-        if (v & FL_SOLID) continue;
-        nf++;
-        ns += (v & FL_SPECIAL) != 0;
-        nl += (v & FL_LINK) != 0;
-        nst += (v & FL_STORE) != 0;
+    // per-class counts (on the device) and zeroed link forces
+    {
+        unsigned long long* cnt = nullptr;
+        CK(ctx_alloc_bytes(c, (void**)&cnt, 4 * sizeof(unsigned long long)));
+        unsigned long long h[4] = {0, 0, 0, 0};
+        cudaError_t e = cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), c->stream);
+        if (e == cudaSuccess) e = setup_count_flags(c->flags, E, cnt, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        ctx_free(c, cnt);
+        CK(e);
+        for (int k = 0; k < 4; k++) c->counts[k] = (long long)h[k];
     }
-    c->counts[0] = nf;
-    c->counts[1] = ns;
-    c->counts[2] = nl;
-    c->counts[3] = nst;
     for (int a = 0; a < 3; a++) CK(cudaMemsetAsync(c->fw[a], 0, sizeof(float) * E, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->dirty = false;
@@ -537,11 +539,7 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
         a.fin_s[q] = reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(a.fin_q[q]) -
                                                    (uintptr_t)(pull * (long long)c->tsize));
         a.fout_q[q] = static_cast<char*>(a.f_out) + plane;
-        a.pull_b[q] = (long long)plane - pull * (long long)c->tsize;
-        a.plane_b[q] = (long long)plane;
     }
-    a.fin_base = static_cast<const char*>(a.f_in);
-    a.fout_base = static_cast<char*>(a.f_out);
     float* const* mp = c->macro[msrc];
     float* const* mn = c->macro[1 - msrc];
     a.rho_p = mp[0];
@@ -555,6 +553,7 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
     a.w_n = mn[3];
     a.tau_n = mn[4];
     a.store_all = p->store_fields == 2;
+    a.bulk_kind = c->Q == 19 ? c->bulk_kind : 0;
 }
 
 extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
@@ -659,6 +658,7 @@ extern "C" int lbffs_synchronize(lbffs_ctx* c)
     if (c->timing) harvest_timing(c);
     int h = 0;
     CK(cudaMemcpy(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h & 2) return fail(c, LBFFS_E_CUDA, "a bulk-copy wait of the row-staged step kernel ran out");
     if (h) return fail(c, LBFFS_E_NONFINITE, "non-finite density produced by the step (divergence)");
     return LBFFS_OK;
 }
@@ -877,5 +877,12 @@ extern "C" int lbffs_init_rest(lbffs_ctx* c)
         }
     }
     CK(cudaStreamSynchronize(c->stream));
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_set_bulk_kernel(lbffs_ctx* c, int kind)
+{
+    if (!c || kind < 0 || kind > 1) return fail(c, LBFFS_E_ARG, "lbffs_set_bulk_kernel: kind must be 0 or 1");
+    c->bulk_kind = kind;
     return LBFFS_OK;
 }

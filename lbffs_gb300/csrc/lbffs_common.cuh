@@ -145,11 +145,6 @@ struct PadGeom {
     long long pE;
 };
 
-// threads of one ghost-layer fill: one per cell of each of the six faces
-__host__ __device__ inline long long halo_threads(const PadGeom& g)
-{
-    return 2LL * ((long long)g.ny * g.nz + (long long)g.nx * g.nz + (long long)g.nx * g.ny);
-}
 
 // ---- kernel argument block ----
 struct StepArgs {
@@ -171,6 +166,7 @@ struct StepArgs {
     float omega0, dpdx, les, omega_b, spz, clim, cs;
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity
     int store_all;    // store rho/u/v/w/tau for every fluid cell this step
+    int bulk_kind;    // D3Q19 bulk kernel: 0 per-thread loads, 1 row-staged bulk copies (launch choice)
     int sgs, wall;    // Sgs / Wall selections (runtime in the boundary kernel)
     const int* ibm_box;  // device int[6] lo/hi of the marker box (cells inside store macroscopics), or null
     int* err;            // device error word (non-finite density seen), may be null
@@ -183,12 +179,6 @@ struct StepArgs {
     const void* fin_q[27];
     const void* fin_s[27];
     void* fout_q[27];
-    // the same as byte offsets from one base per copy, for the bulk kernel's single row pointer:
-    // pulled value fin_base + ip*size + pull_b[q], own output fout_base + ip*size + plane_b[q]
-    const char* fin_base;
-    char* fout_base;
-    long long pull_b[27];
-    long long plane_b[27];
 };
 
 __host__ __device__ __forceinline__ int pidx(const StepArgs& a, int i, int j, int k)

@@ -1,9 +1,10 @@
 // lbffs_server_*: continuous batching of many lattice solves on one GPU.
 //
-// A loop thread owns the GPU work.  Each round it
-//   1. admits queued cases while slots and the HBM arena allow: a case becomes an ordinary
-//      context whose buffers are carved from the arena (on the set-up stream, while the previous
-//      round runs), gets its arrays uploaded and its geometry committed, and starts at step 0;
+// An admission thread brings queued cases in while slots and the HBM arena allow: a case becomes
+// an ordinary context whose buffers are carved from the arena, gets its arrays uploaded and its
+// geometry committed on the set-up stream (while the batch computes), and is handed over ready at
+// step 0.  A loop thread owns the batched GPU work.  Each round it
+//   1. moves the ready cases into the batch;
 //   2. when the resident set changed, rebuilds the batch tables (per group of storage format and
 //      LES switch: the cases' kernel arguments for both parities, the prefix sums of bulk tiles
 //      and special cells) and captures steps_per_round steps into a CUDA graph;
@@ -28,6 +29,7 @@
 
 #include "batch.h"
 #include "ctx.h"
+#include "step_kernels.cuh"
 
 using namespace lbffs;
 
@@ -83,11 +85,13 @@ cudaError_t grow(T** p, size_t& cap, size_t n)
 
 struct lbffs_server {
     lbffs_server_desc d{};
-    cudaStream_t stream = nullptr;        // batched steps (graph replay)
-    cudaStream_t setup_stream = nullptr;  // per-case uploads, commits and result downloads
+    cudaStream_t stream = nullptr;         // batched steps (graph replay)
+    cudaStream_t setup_stream = nullptr;   // admission: per-case uploads and commits
+    cudaStream_t result_stream = nullptr;  // retirement: result downloads
     void* arena_mem = nullptr;
     std::unique_ptr<Arena> arena;
-    float* stage = nullptr;
+    float* stage = nullptr;   // admission staging
+    float* stage2 = nullptr;  // retirement staging
     size_t stage_elems = 0;
     long long* d_done = nullptr;
     long long* h_done = nullptr;  // pinned
@@ -101,10 +105,12 @@ struct lbffs_server {
     cudaGraphExec_t exec = nullptr;
     bool rebuild = true;
 
-    std::thread loop;
+    std::thread loop, admitter;
     std::mutex mu;
-    std::condition_variable cv;       // wakes the loop (new work / stop)
+    std::condition_variable cv;       // wakes the loop (cases ready / stop)
+    std::condition_variable admit_cv; // wakes the admitter (submission / memory or slot freed / stop)
     std::condition_variable done_cv;  // wakes waiters (a case finished)
+    std::vector<Request*> ready;      // admitted and set up, not yet in the batch
     bool stop = false;
     std::deque<Request*> queue;
     std::vector<Request*> resident;
@@ -112,6 +118,7 @@ struct lbffs_server {
     std::map<long long, std::unique_ptr<Request>> all;
     long long next_id = 1;
     std::string err = "no error";
+    bool admit_poke = true;  // a submission or a change the admitter has not looked at yet
 
     // statistics
     long long submitted = 0, completed = 0, failed = 0, rounds = 0, graph_builds = 0;
@@ -166,8 +173,11 @@ bool admit_one(lbffs_server* s, Request* r)
     }
     c->fcur = c->mcur = 0;
     r->ctx = c;
-    r->slot = s->free_slots.back();
-    s->free_slots.pop_back();
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        r->slot = s->free_slots.back();
+        s->free_slots.pop_back();
+    }
     // the slot is in no captured graph (it was freed only after a rebuild dropped its last case)
     s->h_done[r->slot] = 0;
     cudaMemcpyAsync(s->d_done + r->slot, s->h_done + r->slot, sizeof(long long), cudaMemcpyHostToDevice,
@@ -178,34 +188,51 @@ bool admit_one(lbffs_server* s, Request* r)
     return true;
 }
 
-void admit(lbffs_server* s)
+// Admission thread: brings queued cases to step 0 on the set-up stream while the loop thread keeps
+// the GPU busy with the resident batch.  First fit over the queue: a case that does not fit the
+// arena now waits for a retirement, later smaller cases may pass it.
+void run_admitter(lbffs_server* s)
 {
-    std::vector<Request*> cand;
-    {
-        std::lock_guard<std::mutex> lock(s->mu);
-        cand.assign(s->queue.begin(), s->queue.end());
-    }
-    std::vector<Request*> taken;
-    for (Request* r : cand) {
-        if ((int)s->resident.size() >= s->d.max_cases) break;
-        if (!admit_one(s, r)) continue;  // does not fit now: later, smaller requests may
-        taken.push_back(r);
-        if (r->state == LBFFS_CASE_RUNNING) {
+    cudaSetDevice(s->d.device);
+    long long seen_retired = -1;
+    for (;;) {
+        std::vector<Request*> cand;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            // wait for a submission or for memory / a slot freed since the last unsuccessful pass
+            s->admit_cv.wait(lock, [&] {
+                return s->stop || (!s->queue.empty() && !s->free_slots.empty() &&
+                                   (seen_retired != s->completed + s->failed || s->admit_poke));
+            });
+            if (s->stop) return;
+            s->admit_poke = false;
+            seen_retired = s->completed + s->failed;
+            cand.assign(s->queue.begin(), s->queue.end());
+        }
+        bool any = false;
+        for (Request* r : cand) {
+            {
+                std::lock_guard<std::mutex> lock(s->mu);
+                if (s->free_slots.empty() || s->stop) break;
+            }
+            if (!admit_one(s, r)) continue;  // does not fit now
+            any = true;
             std::lock_guard<std::mutex> lock(s->mu);
-            s->resident.push_back(r);
-            s->rebuild = true;
+            s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
+            if (r->state == LBFFS_CASE_FAILED) {
+                s->failed++;
+                r->t_done = now_s();
+                s->done_cv.notify_all();
+            } else {
+                s->ready.push_back(r);
+                s->cv.notify_all();
+            }
+        }
+        if (any) {
+            std::lock_guard<std::mutex> lock(s->mu);
+            s->admit_poke = true;  // the queue changed: look again at once
         }
     }
-    if (taken.empty()) return;
-    std::lock_guard<std::mutex> lock(s->mu);
-    for (Request* r : taken) {
-        s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
-        if (r->state == LBFFS_CASE_FAILED) {
-            s->failed++;
-            r->t_done = now_s();
-        }
-    }
-    s->done_cv.notify_all();
 }
 
 cudaError_t build_batch(lbffs_server* s)
@@ -244,9 +271,10 @@ cudaError_t build_batch(lbffs_server* s)
             hc[i].nsteps = r->nsteps;
             hc[i].slot = r->slot;
             hc[i].tiles_x = (c->d.nx + BULK_BX * BULK_V - 1) / (BULK_BX * BULK_V);
-            tiles[i + 1] = tiles[i] + hc[i].tiles_x * c->d.ny * c->d.nz;
+            hc[i].tiles = hc[i].tiles_x * c->d.ny * c->d.nz;
+            tiles[i + 1] = tiles[i] + (hc[i].tiles + BATCH_TILES_PER_CTA - 1) / BATCH_TILES_PER_CTA;
             sp[i + 1] = sp[i] + c->n_special;
-            hl[i + 1] = hl[i] + halo_threads(c->pg);
+            hl[i + 1] = hl[i] + halo_blocks(c->pg, 19, 0) + halo_blocks(c->pg, 19, 1) + halo_blocks(c->pg, 19, 2);
         }
         size_t cap = g.cap;
         if (n + 1 > (int)g.cap || !g.d_cases) {
@@ -325,6 +353,8 @@ cudaError_t build_batch(lbffs_server* s)
 void retire(lbffs_server* s, Request* r)
 {
     lbffs_ctx* c = r->ctx;
+    c->stream = s->result_stream;  // no work of this case is pending on the set-up stream
+    c->stage = s->stage2;
     const long long parity = r->nsteps & 1;
     c->fcur = c->mcur = (int)parity;
     const size_t E = (size_t)c->E;
@@ -346,9 +376,9 @@ void retire(lbffs_server* s, Request* r)
     else if (err_word) r->err = "non-finite density (divergence)";
     lbffs_destroy(c);
     r->ctx = nullptr;
+    std::lock_guard<std::mutex> lock(s->mu);
     s->free_slots.push_back(r->slot);
     r->slot = -1;
-    std::lock_guard<std::mutex> lock(s->mu);
     r->t_done = now_s();
     r->bnd[0].clear();
     for (auto& v : r->bnd) std::vector<int>().swap(v);
@@ -367,6 +397,7 @@ void retire(lbffs_server* s, Request* r)
         s->failed++;
     }
     s->done_cv.notify_all();
+    s->admit_cv.notify_all();  // memory and a slot came free
 }
 
 void run_loop(lbffs_server* s)
@@ -376,11 +407,16 @@ void run_loop(lbffs_server* s)
         {
             std::unique_lock<std::mutex> lock(s->mu);
             s->cv.wait(lock, [&] {
-                return s->stop || !s->queue.empty() || !s->resident.empty() || !s->to_retire.empty();
+                return s->stop || !s->ready.empty() || !s->resident.empty() || !s->to_retire.empty();
             });
             if (s->stop) return;
+            // admitted cases join the batch at this round boundary
+            if (!s->ready.empty()) {
+                for (Request* r : s->ready) s->resident.push_back(r);
+                s->ready.clear();
+                s->rebuild = true;
+            }
         }
-        if (s->resident.empty()) admit(s);  // idle GPU: bring cases in before the first round
         bool launched = false;
         if (!s->resident.empty()) {
             if (s->rebuild) {
@@ -415,7 +451,6 @@ void run_loop(lbffs_server* s)
             done_now.swap(s->to_retire);
         }
         for (Request* r : done_now) retire(s, r);
-        if (launched) admit(s);
         if (!launched) continue;
         cudaError_t e = cudaStreamSynchronize(s->stream);
         s->rounds++;
@@ -489,13 +524,13 @@ cudaError_t batch_bulk(int storage, bool les, const BatchCase* cases, const int*
     return cudaErrorInvalidValue;
 }
 
-cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nthreads,
+cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nblocks,
                        const long long* done, cudaStream_t st)
 {
     switch (storage) {
-        case ST_FP32: return batch_halo_s0(cases, h_start, ncases, nthreads, done, st);
-        case ST_FP16S: return batch_halo_s1(cases, h_start, ncases, nthreads, done, st);
-        case ST_BF16S: return batch_halo_s2(cases, h_start, ncases, nthreads, done, st);
+        case ST_FP32: return batch_halo_s0(cases, h_start, ncases, nblocks, done, st);
+        case ST_FP16S: return batch_halo_s1(cases, h_start, ncases, nblocks, done, st);
+        case ST_BF16S: return batch_halo_s2(cases, h_start, ncases, nblocks, done, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -523,9 +558,11 @@ extern "C" int lbffs_server_create(const lbffs_server_desc* desc, lbffs_server**
     cudaError_t e = cudaSetDevice(desc->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->setup_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->result_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&s->arena_mem, desc->hbm_budget);
     s->stage_elems = (size_t)16 << 20;
     if (e == cudaSuccess) e = cudaMalloc(&s->stage, sizeof(float) * s->stage_elems);
+    if (e == cudaSuccess) e = cudaMalloc(&s->stage2, sizeof(float) * s->stage_elems);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_done, sizeof(long long) * desc->max_cases);
     if (e == cudaSuccess) e = cudaMemset(s->d_done, 0, sizeof(long long) * desc->max_cases);
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_done, sizeof(long long) * desc->max_cases);
@@ -538,6 +575,7 @@ extern "C" int lbffs_server_create(const lbffs_server_desc* desc, lbffs_server**
     for (int i = desc->max_cases - 1; i >= 0; i--) s->free_slots.push_back(i);
     lbffs_server* p = s.release();
     p->loop = std::thread(run_loop, p);
+    p->admitter = std::thread(run_admitter, p);
     *out = p;
     return LBFFS_OK;
 }
@@ -550,10 +588,13 @@ extern "C" int lbffs_server_destroy(lbffs_server* s)
         s->stop = true;
     }
     s->cv.notify_all();
+    s->admit_cv.notify_all();
+    if (s->admitter.joinable()) s->admitter.join();
     if (s->loop.joinable()) s->loop.join();
     cudaSetDevice(s->d.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->setup_stream) cudaStreamSynchronize(s->setup_stream);
+    if (s->result_stream) cudaStreamSynchronize(s->result_stream);
     for (auto& kv : s->all)
         if (kv.second->ctx) lbffs_destroy(kv.second->ctx);
     if (s->exec) cudaGraphExecDestroy(s->exec);
@@ -568,10 +609,12 @@ extern "C" int lbffs_server_destroy(lbffs_server* s)
     if (s->d_done) cudaFree(s->d_done);
     if (s->h_done) cudaFreeHost(s->h_done);
     if (s->stage) cudaFree(s->stage);
+    if (s->stage2) cudaFree(s->stage2);
     s->arena.reset();
     if (s->arena_mem) cudaFree(s->arena_mem);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->setup_stream) cudaStreamDestroy(s->setup_stream);
+    if (s->result_stream) cudaStreamDestroy(s->result_stream);
     delete s;
     return LBFFS_OK;
 }
@@ -618,8 +661,9 @@ extern "C" int lbffs_server_submit(lbffs_server* s, const lbffs_case* c, long lo
         s->queue.push_back(r.get());
         s->all[r->id] = std::move(r);
         s->submitted++;
+        s->admit_poke = true;
     }
-    s->cv.notify_all();
+    s->admit_cv.notify_all();
     return LBFFS_OK;
 }
 

@@ -5,6 +5,8 @@
 // geometry change into a u16 boundary word and a u8 flag per cell plus a compact list
 // of the cells that need the general boundary path; the time step never touches the
 // int32 arrays again.
+#include <climits>
+
 #include "launch.h"
 #include "step_kernels.cuh"
 
@@ -281,27 +283,82 @@ cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long 
     return cudaErrorInvalidValue;
 }
 
-// ---- ghost layer (halo_thread in step_kernels.cuh) over the six faces ----
+// ---- ghost layer (halo_block in step_kernels.cuh) ----
 template <int Q, typename W>
-__global__ void __launch_bounds__(128) k_halo(W* f, const uint8_t* __restrict__ flags, const uint16_t* __restrict__ bc,
-                                              PadGeom g, long long n)
+__global__ void __launch_bounds__(HALO_BS) k_halo(W* f, const uint8_t* __restrict__ flags,
+                                                  const uint16_t* __restrict__ bc, PadGeom g)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) halo_thread<Q, W>(f, flags, bc, g, t);
+    halo_block<Q, W>(f, flags, bc, g, blockIdx.x, threadIdx.x);
 }
 
 cudaError_t halo_fill(int Q, int tsize, void* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
                       cudaStream_t st)
 {
-    const long long n = halo_threads(g);
-    const unsigned nb = (unsigned)((n + 127) / 128);
+    const long long nb = halo_blocks(g, Q, 0) + halo_blocks(g, Q, 1) + halo_blocks(g, Q, 2);
     if (Q == 19) {
-        if (tsize == 4) k_halo<19, uint32_t><<<nb, 128, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g, n);
-        else k_halo<19, uint16_t><<<nb, 128, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g, n);
+        if (tsize == 4) k_halo<19, uint32_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g);
+        else k_halo<19, uint16_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g);
     } else {
-        if (tsize == 4) k_halo<27, uint32_t><<<nb, 128, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g, n);
-        else k_halo<27, uint16_t><<<nb, 128, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g, n);
+        if (tsize == 4) k_halo<27, uint32_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g);
+        else k_halo<27, uint16_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g);
     }
+    return cudaGetLastError();
+}
+
+// Boundary-code check over the three per-axis code arrays: out[0] bit 0 = a WallFunction code
+// (7) is present, bit 1 = a value outside {0, 1, 3, 4, 5, 6, 7} is present, out[1] = the largest
+// such value.
+__global__ void k_check_codes(const int* __restrict__ b1, const int* __restrict__ b2, const int* __restrict__ b3,
+                              long long E, int* out)
+{
+    int bits = 0, bad = INT_MIN;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < E; i += (long long)gridDim.x * blockDim.x) {
+        const int v[3] = {b1[i], b2[i], b3[i]};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (v[d] == BC_WALLFN) bits |= 1;
+            else if (!(v[d] == 0 || v[d] == 1 || v[d] == 3 || v[d] == 4 || v[d] == 5 || v[d] == 6)) {
+                bits |= 2;
+                bad = max(bad, v[d]);
+            }
+        }
+    }
+    bits = __reduce_or_sync(0xffffffffu, bits);
+    bad = __reduce_max_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && bits) {
+        atomicOr(out, bits);
+        atomicMax(out + 1, bad);
+    }
+}
+
+cudaError_t setup_check_codes(const int* b1, const int* b2, const int* b3, long long E, int* out, cudaStream_t st)
+{
+    k_check_codes<<<512, 256, 0, st>>>(b1, b2, b3, E, out);
+    return cudaGetLastError();
+}
+
+// Cells per class: counts[0] fluid, [1] special, [2] STL-link, [3] storing macroscopics.
+__global__ void k_count_flags(const uint8_t* __restrict__ flags, long long E, unsigned long long* counts)
+{
+    unsigned c[4] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < E; i += (long long)gridDim.x * blockDim.x) {
+        const uint8_t v = flags[i];
+        if (v & FL_SOLID) continue;
+        c[0]++;
+        c[1] += (v & FL_SPECIAL) != 0;
+        c[2] += (v & FL_LINK) != 0;
+        c[3] += (v & FL_STORE) != 0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const unsigned t = __reduce_add_sync(0xffffffffu, c[k]);
+        if ((threadIdx.x & 31) == 0 && t) atomicAdd(counts + k, (unsigned long long)t);
+    }
+}
+
+cudaError_t setup_count_flags(const uint8_t* flags, long long E, unsigned long long* counts, cudaStream_t st)
+{
+    k_count_flags<<<512, 256, 0, st>>>(flags, E, counts);
     return cudaGetLastError();
 }
 

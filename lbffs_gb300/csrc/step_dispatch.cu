@@ -44,6 +44,12 @@ static int part_of(const StepConfig& c, bool bulk)
 cudaError_t launch_q19(const StepArgs& a, const StepConfig& c, bool bulk, cudaStream_t st)
 {
     if (c.storage < 0 || c.storage > 2) return cudaErrorInvalidValue;
+    if (bulk && a.bulk_kind == 1) {
+        const bool les = c.sgs != SGS_WALE && c.les;
+        if (c.storage == ST_FP32) return launch_bulk_tma_s0(a, c.sgs, les, st);
+        if (c.storage == ST_FP16S) return launch_bulk_tma_s1(a, c.sgs, les, st);
+        return launch_bulk_tma_s2(a, c.sgs, les, st);
+    }
     return k19[c.storage][part_of(c, bulk)](a, st);
 }
 

@@ -199,14 +199,13 @@ __device__ __forceinline__ int missing_dir(int q, const int (&b)[3])
     return out;
 }
 
-// The bulk step of one fluid cell whose Q populations are already in ft (held form for D3Q19):
-// macroscopics, eddy viscosity, sponge, collision, and the Q streaming stores at ip.
+// The collision of one bulk cell whose Q pulled populations are in ft (held form for D3Q19):
+// macroscopics, eddy viscosity, sponge, stores of the macroscopic fields that are read later, and
+// the collision in place.
 template <int Q, int S, int COLL, int SGS, bool LES>
-__device__ __forceinline__ void bulk_cell(const StepArgs& a, float (&ft)[Q], uint8_t fl, int i, int j, int k, int ic,
-                                          int ip)
+__device__ __forceinline__ void bulk_collide(const StepArgs& a, float (&ft)[Q], uint8_t fl, int i, int j, int k,
+                                             int ic)
 {
-    using T = typename Codec<S>::T;
-    constexpr bool HELD = (Q == 19);
     const float omega = (fl & FL_OMEGA) ? __ldg(a.omega + ic) : a.omega0;
     float rho, u, v, w, tsgs = 0.f;
     if constexpr (Q == 19) {
@@ -258,10 +257,19 @@ __device__ __forceinline__ void bulk_cell(const StepArgs& a, float (&ft)[Q], uin
         }
         collide<Q, COLL>(ft, rho, u, v, w, we, a);
     }
-    char* pout = a.fout_base + (long long)ip * (long long)sizeof(T);
+}
+
+// The bulk step of one fluid cell: bulk_collide, then the Q streaming stores at ip.
+template <int Q, int S, int COLL, int SGS, bool LES>
+__device__ __forceinline__ void bulk_cell(const StepArgs& a, float (&ft)[Q], uint8_t fl, int i, int j, int k, int ic,
+                                          int ip)
+{
+    using T = typename Codec<S>::T;
+    constexpr bool HELD = (Q == 19);
+    bulk_collide<Q, S, COLL, SGS, LES>(a, ft, fl, i, j, k, ic);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-        T* p = reinterpret_cast<T*>(pout + a.plane_b[q]);
+        T* p = static_cast<T*>(a.fout_q[q]) + ip;
         if constexpr (HELD) Codec<S>::store_held(p, ft[q]);
         else Codec<S>::store(p, ft[q], lat_w(Q, q));
     }
@@ -296,10 +304,10 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
 #pragma unroll
     for (int v = 0; v < BULK_V; v++) {
         if (!act[v]) continue;
-        const char* pin = a.fin_base + (long long)(prow + i0 + 32 * v) * (long long)sizeof(T);
+        const int ip = prow + i0 + 32 * v;
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            const T* p = reinterpret_cast<const T*>(pin + a.pull_b[q]);
+            const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
             ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
         }
     }
@@ -515,148 +523,178 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
     if (t < a.n_special) special_cell<Q, S, COLL>(a, t);
 }
 
-// missing_dir for a direction q known at compile time: every lattice lookup is a constant
-template <int Q, int q>
-__device__ __forceinline__ int missing_dir_ct(const int (&b)[3])
-{
-    constexpr int c0 = lat_c(Q, q, 0), c1 = lat_c(Q, q, 1), c2 = lat_c(Q, q, 2);
-    constexpr int r = lat_opp(Q, q);
-    constexpr int mx = c0 ? lat_find(Q, -c0, c1, c2) : r;
-    constexpr int my = c1 ? lat_find(Q, c0, -c1, c2) : r;
-    constexpr int mz = c2 ? lat_find(Q, c0, c1, -c2) : r;
-    if constexpr (Q == 19) {
-        if constexpr ((c0 != 0) + (c1 != 0) + (c2 != 0) < 2) {
-            return r;
-        } else {
-            if (c0 != 0 && b[0] == BC_SYM) return mx;  // first Symmetry axis among the nonzero components
-            if (c1 != 0 && b[1] == BC_SYM) return my;
-            if (c2 != 0 && b[2] == BC_SYM) return mz;
-            return r;
-        }
-    } else {
-        int out = r;  // the last Symmetry axis wins; a zero component falls back to reflection
-        if (b[0] == BC_SYM) out = mx;
-        if (b[1] == BC_SYM) out = my;
-        if (b[2] == BC_SYM) out = mz;
-        return out;
-    }
-}
-
 // ---- ghost layer: the reference's face streaming for populations that cross the grid edge ----
 // Every population q of a cell P whose upwind neighbour P - c_q lies outside the grid is pulled
 // from the ghost P - c_q.  The ghost holds the value upwindID_B / reflectOrMirrorQ would pull
 // (D3Q19 kernel.cl:114-575, D3Q27 kernel.cl:1133-1146): the periodically wrapped upwind cell's
 // value, or, when a crossed face of P carries a wall code, P's own value of the bounce-back /
-// mirror direction.  The fill runs over the six faces of the grid: one thread per cell of a face
-// handles the directions that cross that face outward-in (5 for D3Q19, 9 for D3Q27), gathering
-// all of them before writing.  A diagonal crossing two faces at an edge is handled by both face
-// threads with the same value.  Raw element copies (W: the element's bit pattern): no rounding.
-// compile-time loop: f(std::integral_constant<int, I>) for I in [I0, N)
-template <int I0, int N, class F>
-__device__ __forceinline__ void static_for(F&& f)
-{
-    if constexpr (I0 < N) {
-        f(std::integral_constant<int, I0>{});
-        static_for<I0 + 1, N>(f);
-    }
-}
-
-template <int Q, int AXIS, int SIGN>
-__host__ __device__ constexpr int side_dir(int n)
-{
-    // the n-th direction q with c_q[AXIS] == SIGN
-    for (int q = 1, m = 0; q < Q; q++)
-        if (lat_c(Q, q, AXIS) == SIGN) {
-            if (m == n) return q;
-            m++;
-        }
-    return -1;
-}
-
+// mirror direction.  The fill runs over the six faces of the grid: each thread takes one face cell
+// and the directions that cross its face outward-in (5 for D3Q19, 9 for D3Q27).  A diagonal
+// crossing two faces at an edge is written by both faces' threads with the same value.  Raw
+// element copies (W: the element's bit pattern): no rounding.
 template <int Q>
 __host__ __device__ constexpr int side_count()
 {
     return Q == 19 ? 5 : 9;
 }
 
-// Face thread: cell x on the face AXIS = (SIGN > 0 ? 0 : N - 1), which pulls across that face the
-// directions with c[AXIS] == SIGN.
-template <int Q, typename W, int AXIS, int SIGN>
-__device__ __forceinline__ void halo_face_cell(W* f, const uint8_t* __restrict__ flags, const uint16_t* __restrict__ bc,
-                                               const int (&x)[3], const PadGeom& g)
+__host__ __device__ constexpr int side_count_rt(int Q) { return Q == 19 ? 5 : 9; }
+
+// Direction tables of the ghost fill, read per block from constant memory (one short code path
+// for every face and direction instead of one unrolled variant each, which keeps the kernel in
+// the instruction cache): velocity, the bounce-back and the three mirror directions.
+struct HaloDir {
+    signed char c[3];
+    signed char opp, mx, my, mz;  // reflection; mirror across x / y / z (the reflection where c_d = 0)
+    signed char nonzero;          // number of nonzero components
+};
+
+template <int Q>
+struct HaloTable {
+    HaloDir d[27];
+    signed char side[3][2][9];  // [axis][low / high face][n]: the directions crossing that face inward
+    constexpr HaloTable() : d{}, side{}
+    {
+        for (int q = 0; q < Q; q++) {
+            const int c0 = lat_c(Q, q, 0), c1 = lat_c(Q, q, 1), c2 = lat_c(Q, q, 2);
+            const int r = lat_opp(Q, q);
+            d[q].c[0] = (signed char)c0;
+            d[q].c[1] = (signed char)c1;
+            d[q].c[2] = (signed char)c2;
+            d[q].opp = (signed char)r;
+            d[q].mx = (signed char)(c0 ? lat_find(Q, -c0, c1, c2) : r);
+            d[q].my = (signed char)(c1 ? lat_find(Q, c0, -c1, c2) : r);
+            d[q].mz = (signed char)(c2 ? lat_find(Q, c0, c1, -c2) : r);
+            d[q].nonzero = (signed char)((c0 != 0) + (c1 != 0) + (c2 != 0));
+        }
+        for (int ax = 0; ax < 3; ax++)
+            for (int hi = 0; hi < 2; hi++) {
+                int m = 0;
+                for (int q = 1; q < Q; q++)
+                    if (lat_c(Q, q, ax) == (hi ? -1 : 1)) side[ax][hi][m++] = (signed char)q;
+            }
+    }
+};
+
+__constant__ const HaloTable<19> kHalo19{};
+__constant__ const HaloTable<27> kHalo27{};
+
+template <int Q>
+__device__ __forceinline__ const HaloTable<Q>& halo_table()
 {
+    if constexpr (Q == 19) return kHalo19;
+    else return kHalo27;
+}
+
+// reflectOrMirrorQ with the run-time direction dq and the cell's face codes b (missing_dir)
+template <int Q>
+__device__ __forceinline__ int halo_missing(const HaloDir& dq, const int (&b)[3])
+{
+    if (Q == 19) {
+        if (dq.nonzero < 2) return dq.opp;
+        if (dq.c[0] != 0 && b[0] == BC_SYM) return dq.mx;  // first Symmetry axis among the nonzero components
+        if (dq.c[1] != 0 && b[1] == BC_SYM) return dq.my;
+        if (dq.c[2] != 0 && b[2] == BC_SYM) return dq.mz;
+        return dq.opp;
+    }
+    int out = dq.opp;  // the last Symmetry axis wins; a zero component falls back to reflection
+    if (b[0] == BC_SYM) out = dq.mx;
+    if (b[1] == BC_SYM) out = dq.my;
+    if (b[2] == BC_SYM) out = dq.mz;
+    return out;
+}
+
+// Ghost fill work of one lattice: for each axis, its two faces in blocks of HALO_BS face cells.
+// Block b of the flattened grid: axis, face (low / high) and run of cells; thread: one face cell,
+// which fills the ghosts of all NQ directions it pulls across that face (its flags and boundary
+// word are read once; the NQ source values are gathered before the ghosts are written).
+constexpr int HALO_BS = 128;
+
+__host__ __device__ inline long long halo_face_cells(const PadGeom& g, int axis)
+{
+    return axis == 0 ? (long long)g.ny * g.nz : axis == 1 ? (long long)g.nx * g.nz : (long long)g.nx * g.ny;
+}
+
+__host__ __device__ inline long long halo_blocks(const PadGeom& g, int /*Q*/, int axis)
+{
+    return 2LL * ((halo_face_cells(g, axis) + HALO_BS - 1) / HALO_BS);
+}
+
+template <int Q, typename W>
+__device__ __forceinline__ void halo_block(W* f, const uint8_t* __restrict__ flags, const uint16_t* __restrict__ bc,
+                                           const PadGeom& g, long long b, int tid)
+{
+    constexpr int NQ = side_count<Q>();
+    int axis = 0;
+    long long blk = b;
+    long long nb = halo_blocks(g, Q, 0);
+    if (blk >= nb) {
+        blk -= nb;
+        axis = 1;
+        nb = halo_blocks(g, Q, 1);
+        if (blk >= nb) {
+            blk -= nb;
+            axis = 2;
+        }
+    }
+    const long long cells = halo_face_cells(g, axis);
+    const long long per = (cells + HALO_BS - 1) / HALO_BS;
+    const int hi = blk >= per ? 1 : 0;
+    const long long p = (blk - hi * per) * HALO_BS + tid;
+    if (p >= cells) return;
     const int N[3] = {g.nx, g.ny, g.nz};
+    // face cell: the face coordinate on axis, the other two from p in row-major order
+    const int a0 = axis == 0 ? 1 : 0, a1 = axis == 2 ? 1 : 2;
+    int x[3];
+    x[axis] = hi ? N[axis] - 1 : 0;
+    x[a0] = (int)(p % N[a0]);
+    x[a1] = (int)(p / N[a0]);
     const long long ic = ((long long)x[2] * g.ny + x[1]) * g.nx + x[0];
-    if (__ldg(flags + ic) & FL_SOLID) return;  // nobody pulls through a solid cell's ghosts
+    const uint8_t fl = __ldg(flags + ic);  // both loads in flight together
     const uint16_t bw = __ldg(bc + ic);
-    const int b[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
+    if (fl & FL_SOLID) return;  // nobody pulls through a solid cell's ghosts
+    const int bcode[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
     const bool face = (bw >> 9) & 1;
     const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
-    constexpr int NQ = side_count<Q>();
+    const HaloTable<Q>& tab = halo_table<Q>();
     W v[NQ];
-    static_for<0, NQ>([&](auto n) {
-        constexpr int q = side_dir<Q, AXIS, SIGN>(decltype(n)::value);
+    long long dst[NQ];
+#pragma unroll
+    for (int n = 0; n < NQ; n++) {
+        const int q = tab.side[axis][hi][n];
+        const HaloDir dq = tab.d[q];
         int up[3];
         bool miss = false;
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            up[d] = x[d] - lat_c(Q, q, d);
+            up[d] = x[d] - dq.c[d];
             if (up[d] < 0) {
-                miss |= face && is_wall_code(b[d]);
+                miss |= face && is_wall_code(bcode[d]);
                 up[d] += N[d];
             } else if (up[d] >= N[d]) {
-                miss |= face && is_wall_code(b[d]);
+                miss |= face && is_wall_code(bcode[d]);
                 up[d] -= N[d];
             }
         }
-        v[decltype(n)::value] = miss ? __ldg(f + (long long)missing_dir_ct<Q, q>(b) * g.pE + ip)
-                                     : __ldg(f + (long long)q * g.pE + g.porg + up[2] * g.pxy + up[1] * g.px + up[0]);
-    });
-    static_for<0, NQ>([&](auto n) {
-        constexpr int q = side_dir<Q, AXIS, SIGN>(decltype(n)::value);
-        constexpr int cx = lat_c(Q, q, 0), cy = lat_c(Q, q, 1), cz = lat_c(Q, q, 2);
-        f[(long long)q * g.pE + ip - (cx + cy * g.px + cz * g.pxy)] = v[decltype(n)::value];
-    });
-}
-
-// Thread t of the ghost fill of one lattice (t < halo_threads(g)): faces in the order x-, x+,
-// y-, y+, z-, z+, each face a plane of cells in its own row-major order.
-template <int Q, typename W>
-__device__ __forceinline__ void halo_thread(W* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
-                                            long long t)
-{
-    const long long ax = (long long)g.ny * g.nz, ay = (long long)g.nx * g.nz, az = (long long)g.nx * g.ny;
-    int x[3];
-    if (t < 2 * ax) {
-        const bool hi = t >= ax;
-        const long long p = hi ? t - ax : t;
-        x[0] = hi ? g.nx - 1 : 0;
-        x[1] = (int)(p % g.ny);
-        x[2] = (int)(p / g.ny);
-        if (hi) halo_face_cell<Q, W, 0, -1>(f, flags, bc, x, g);
-        else halo_face_cell<Q, W, 0, 1>(f, flags, bc, x, g);
-        return;
+        v[n] = miss ? __ldg(f + (long long)halo_missing<Q>(dq, bcode) * g.pE + ip)
+                    : __ldg(f + (long long)q * g.pE + g.porg + up[2] * g.pxy + up[1] * g.px + up[0]);
+        dst[n] = (long long)q * g.pE + ip - (dq.c[0] + dq.c[1] * g.px + dq.c[2] * g.pxy);
     }
-    t -= 2 * ax;
-    if (t < 2 * ay) {
-        const bool hi = t >= ay;
-        const long long p = hi ? t - ay : t;
-        x[0] = (int)(p % g.nx);
-        x[1] = hi ? g.ny - 1 : 0;
-        x[2] = (int)(p / g.nx);
-        if (hi) halo_face_cell<Q, W, 1, -1>(f, flags, bc, x, g);
-        else halo_face_cell<Q, W, 1, 1>(f, flags, bc, x, g);
-        return;
-    }
-    t -= 2 * ay;
-    if (t < 2 * az) {
-        const bool hi = t >= az;
-        const long long p = hi ? t - az : t;
-        x[0] = (int)(p % g.nx);
-        x[1] = (int)(p / g.nx);
-        x[2] = hi ? g.nz - 1 : 0;
-        if (hi) halo_face_cell<Q, W, 2, -1>(f, flags, bc, x, g);
-        else halo_face_cell<Q, W, 2, 1>(f, flags, bc, x, g);
+    // an x ghost sits alone in the padding sector before / after its row: writing the whole
+    // 32-byte sector avoids a read-modify-write of a partly written sector
+    constexpr int A = 32 / (int)sizeof(W);
+    const bool whole = axis == 0 && (!hi || (g.nx % A) == 0);
+#pragma unroll
+    for (int n = 0; n < NQ; n++) {
+        if (whole) {
+            W* sec = f + (hi ? dst[n] : dst[n] - (A - 1));
+            const uint32_t w32 = sizeof(W) == 4 ? (uint32_t)v[n] : ((uint32_t)v[n] | ((uint32_t)v[n] << 16));
+            const uint4 quad = make_uint4(w32, w32, w32, w32);
+            reinterpret_cast<uint4*>(sec)[0] = quad;
+            reinterpret_cast<uint4*>(sec)[1] = quad;
+        } else {
+            f[dst[n]] = v[n];
+        }
     }
 }
 

@@ -51,26 +51,33 @@ def faces():
 
 
 VOXEL_CASES = {
-    # name: (q, nx, ny, nz, mesh builder)
+    # name: (q, nx, ny, nz, mesh builder[, invertFluidSolid])
     "ellipsoid_q19": (19, 40, 32, 30, lambda: G.ellipsoid_mesh(7, 18, 36, (19.3, 15.6, 14.8), (11.0, 8.0, 7.5))),
     "ellipsoid_q27": (27, 40, 32, 30, lambda: G.ellipsoid_mesh(11, 18, 36, (20.1, 16.2, 15.1), (12.0, 9.0, 8.0))),
+    "ellipsoid_big_q19": (19, 96, 80, 72,
+                          lambda: G.ellipsoid_mesh(23, 40, 80, (47.7, 39.2, 35.6), (30.0, 22.0, 20.5), noise=0.05)),
+    "ellipsoid_inv_q19": (19, 40, 32, 30, lambda: G.ellipsoid_mesh(31, 18, 36, (19.1, 15.9, 14.6), (13.0, 10.0, 9.0)),
+                          1),
 }
 
 
 def voxels():
     out = {}
     with tempfile.TemporaryDirectory() as td:
-        for name, (q, nx, ny, nz, mesh) in VOXEL_CASES.items():
+        for name, spec in VOXEL_CASES.items():
+            q, nx, ny, nz, mesh = spec[:5]
+            invert = spec[5] if len(spec) > 5 else 0
             stl = os.path.join(td, "walls.stl")
             G.write_ascii_stl(stl, mesh())
             pre = os.path.join(td, "v_")
             # faces: x BounceBack, y BounceBack, z Cyclic (setSDFnearBwalls sees code 1 on x/y)
-            subprocess.run([os.path.join(REF, f"voxel_ref{q}"), stl, str(nx), str(ny), str(nz), "1.0", "0", "1",
-                            "1", "1", "1", "1", "0", "0", pre], check=True, stdout=subprocess.DEVNULL)
+            subprocess.run([os.path.join(REF, f"voxel_ref{q}"), stl, str(nx), str(ny), str(nz), "1.0", str(invert),
+                            "1", "1", "1", "1", "1", "0", "0", pre], check=True, stdout=subprocess.DEVNULL)
             out[f"{name}__solid"] = np.fromfile(pre + "solid.u8", dtype=np.uint8)
             out[f"{name}__nei_solid"] = np.fromfile(pre + "neiSolid.u8", dtype=np.uint8)
             out[f"{name}__sdf"] = np.fromfile(pre + "sdf.f32", dtype=np.float32)
             out[f"{name}__shape"] = np.array([q, nx, ny, nz])
+            out[f"{name}__invert"] = np.array([invert])
             print(name, int(out[f"{name}__solid"].sum()), "solid cells,", int(out[f"{name}__nei_solid"].sum()),
                   "neiSolid cells")
     np.savez_compressed(os.path.join(HERE, "setup_voxels.npz"), **out)
