@@ -247,6 +247,8 @@ def run_serving(n_req, step_scale, device, budget_gb=150.0):
             "MLUPS": tot / t_served / 1e6, "serial_MLUPS": tot / t_plain / 1e6,
             "hbm_frac": bytes_tot / t_served / 1e9 / peak,
             "hbm_peak_GB": st["hbm_peak"] / 1e9, "rounds": st["rounds"], "graph_builds": st["graph_builds"],
+            "gpu_busy_s": st["gpu_busy_s"], "build_s": st["build_s"], "mean_resident": st["mean_resident"],
+            "served_s": t_served,
             "identical_to_serial": bool(same), "compared": len(keep),
             "serial": "one Lattice per request in arrival order, one step per call + synchronize "
                       "(the reference driver's launch + queue.finish per step)"}

@@ -228,6 +228,9 @@ typedef struct lbffs_server_stats {
     double latency_p50_s, latency_p99_s, latency_mean_s, latency_max_s;  /* submit to result */
     double queue_wait_p50_s, queue_wait_p99_s;  /* submit to admission */
     size_t hbm_in_use, hbm_peak, hbm_capacity;
+    double gpu_busy_s;        /* device time of the replayed rounds (CUDA events) */
+    double build_s;           /* host time spent rebuilding batch tables and graphs */
+    double mean_resident;     /* cases in the batch per round, averaged over rounds */
 } lbffs_server_stats;
 
 int lbffs_server_create(const lbffs_server_desc* desc, lbffs_server** out);

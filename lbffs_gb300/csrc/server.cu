@@ -123,6 +123,8 @@ struct lbffs_server {
     // statistics
     long long submitted = 0, completed = 0, failed = 0, rounds = 0, graph_builds = 0;
     double cell_updates = 0, t_first = -1, t_last = 0;
+    double gpu_busy_s = 0, build_s = 0, resident_sum = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<double> latency, queue_wait;
 };
 
@@ -420,7 +422,9 @@ void run_loop(lbffs_server* s)
         bool launched = false;
         if (!s->resident.empty()) {
             if (s->rebuild) {
+                const double tb = now_s();
                 cudaError_t e = build_batch(s);
+                s->build_s += now_s() - tb;
                 if (e != cudaSuccess) {
                     std::lock_guard<std::mutex> lock(s->mu);
                     s->err = std::string("batch build: ") + cudaGetErrorString(e);
@@ -438,7 +442,10 @@ void run_loop(lbffs_server* s)
                 }
                 s->rebuild = false;
             }
+            cudaEventRecord(s->ev0, s->stream);
             cudaGraphLaunch(s->exec, s->stream);
+            cudaEventRecord(s->ev1, s->stream);
+            s->resident_sum += (double)s->resident.size();
             cudaMemcpyAsync(s->h_done, s->d_done, sizeof(long long) * s->d.max_cases, cudaMemcpyDeviceToHost,
                             s->stream);
             launched = true;
@@ -454,6 +461,9 @@ void run_loop(lbffs_server* s)
         if (!launched) continue;
         cudaError_t e = cudaStreamSynchronize(s->stream);
         s->rounds++;
+        float round_ms = 0.f;
+        if (e == cudaSuccess && cudaEventElapsedTime(&round_ms, s->ev0, s->ev1) == cudaSuccess)
+            s->gpu_busy_s += 1e-3 * round_ms;
         if (e != cudaSuccess) {
             std::lock_guard<std::mutex> lock(s->mu);
             s->err = std::string("round: ") + cudaGetErrorString(e);
@@ -559,6 +569,8 @@ extern "C" int lbffs_server_create(const lbffs_server_desc* desc, lbffs_server**
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->setup_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->result_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&s->arena_mem, desc->hbm_budget);
     s->stage_elems = (size_t)16 << 20;
     if (e == cudaSuccess) e = cudaMalloc(&s->stage, sizeof(float) * s->stage_elems);
@@ -615,6 +627,8 @@ extern "C" int lbffs_server_destroy(lbffs_server* s)
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->setup_stream) cudaStreamDestroy(s->setup_stream);
     if (s->result_stream) cudaStreamDestroy(s->result_stream);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
     delete s;
     return LBFFS_OK;
 }
@@ -741,6 +755,9 @@ extern "C" int lbffs_server_get_stats(lbffs_server* s, lbffs_server_stats* o)
     o->hbm_in_use = s->arena ? s->arena->in_use() : 0;
     o->hbm_peak = s->arena ? s->arena->peak() : 0;
     o->hbm_capacity = s->arena ? s->arena->capacity() : 0;
+    o->gpu_busy_s = s->gpu_busy_s;
+    o->build_s = s->build_s;
+    o->mean_resident = s->rounds ? s->resident_sum / (double)s->rounds : 0.0;
     return LBFFS_OK;
 }
 

@@ -36,7 +36,8 @@ class ServerStats(C.Structure):
                 ("graph_builds", C.c_longlong), ("cell_updates", C.c_double), ("elapsed_s", C.c_double),
                 ("latency_p50_s", C.c_double), ("latency_p99_s", C.c_double), ("latency_mean_s", C.c_double),
                 ("latency_max_s", C.c_double), ("queue_wait_p50_s", C.c_double), ("queue_wait_p99_s", C.c_double),
-                ("hbm_in_use", C.c_size_t), ("hbm_peak", C.c_size_t), ("hbm_capacity", C.c_size_t)]
+                ("hbm_in_use", C.c_size_t), ("hbm_peak", C.c_size_t), ("hbm_capacity", C.c_size_t),
+                ("gpu_busy_s", C.c_double), ("build_s", C.c_double), ("mean_resident", C.c_double)]
 
 
 def _bind(lib):
