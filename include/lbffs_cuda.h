@@ -184,6 +184,19 @@ int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
    and NEISOLID fields; the geometry takes effect at the next lbffs_step. */
 int lbffs_voxelize(lbffs_ctx* ctx, const float* vertices, long long ntri, int invert);
 
+/* The LES wall-distance set-up of D3Q19_opencl/ns.cpp:200-225 on the device: the SDF field is set
+   to sdf_ini, setSDF (src/walls.hpp:218-268, one call per STL patch) runs with (dr, p) around the
+   context's current NEISOLID field, then setSDFnearBwalls (walls.hpp:372-467) with dr_walls on
+   the uploaded BOUNDARY1..3 codes (int(dr_walls) < 0 skips it).  ns.cpp passes dr = 10, p = 7,
+   sdf_ini = 10000, dr_walls = 3.  vertices: as for lbffs_voxelize, patches concatenated;
+   normals: 3 floats per triangle, the facet normals as read from the STL; patch_ntri: npatch
+   triangle counts.  Every setSDF call rewrites every near cell, so the result is that of the last
+   patch's call (npatch = 0: no setSDF).  The arithmetic has the reference's types and order; the
+   weight r^-p is computed in double on the device, so a sum may round differently from the host
+   library's pow in rare cells (a float ulp).  Replaces the SDF field. */
+int lbffs_build_sdf(lbffs_ctx* ctx, const float* vertices, const float* normals, const long long* patch_ntri,
+                    int npatch, float dr, float p, float sdf_ini, float dr_walls);
+
 /* Set both population copies to the rest equilibrium rho = 1, u = 0 (f_q = w_q), the state
    initialization.hpp writes for a fluid at rest, without a host upload of F. */
 int lbffs_init_rest(lbffs_ctx* ctx);

@@ -94,6 +94,8 @@ def load_library():
         "lbffs_init_rest": ([vp], i),
         "lbffs_set_bulk_kernel": ([vp, i], i),
         "lbffs_voxelize": ([vp, C.POINTER(C.c_float), C.c_longlong, i], i),
+        "lbffs_build_sdf": ([vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_longlong), i, C.c_float,
+                             C.c_float, C.c_float, C.c_float], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -181,6 +183,22 @@ class Lattice:
         v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 9)
         self._check(self.lib.lbffs_voxelize(self.h, v.ctypes.data_as(C.POINTER(C.c_float)), v.shape[0],
                                             int(bool(invert))))
+
+    def build_sdf(self, vertices, normals, patch_ntri=None, dr=10.0, p=7.0, sdf_ini=10000.0, dr_walls=3.0):
+        """The LES wall-distance field of ns.cpp:200-225 on the device: setSDF per STL patch around
+        the current neiSolid, then setSDFnearBwalls on the uploaded boundary1..3 codes.
+
+        ``vertices``: (ntri, 3, 3) float32 as for :meth:`voxelize`; ``normals``: (ntri, 3) facet
+        normals as read from the STL; ``patch_ntri``: triangles per patch (default: one patch)."""
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 9)
+        n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        if n.shape[0] != v.shape[0]:
+            raise ValueError("one normal per triangle")
+        pn = np.ascontiguousarray([v.shape[0]] if patch_ntri is None else patch_ntri, dtype=np.int64)
+        self._check(self.lib.lbffs_build_sdf(self.h, v.ctypes.data_as(C.POINTER(C.c_float)),
+                                             n.ctypes.data_as(C.POINTER(C.c_float)),
+                                             pn.ctypes.data_as(C.POINTER(C.c_longlong)), int(pn.size), float(dr),
+                                             float(p), float(sdf_ini), float(dr_walls)))
 
     def set_bulk_kernel(self, kind):
         """D3Q19 bulk kernel variant: 0 per-thread loads, 1 row-staged bulk copies (same results)."""

@@ -9,6 +9,9 @@ voxeliser output).
 """
 from __future__ import annotations
 
+import re
+from fractions import Fraction
+
 import numpy as np
 
 SDF_NONE = np.float32(10000.0)
@@ -68,18 +71,68 @@ def ellipsoid_mesh(seed, n_theta, n_phi, center, radii, noise=0.05):
 
 
 def write_ascii_stl(path, tris, name="walls"):
-    """ASCII STL in the layout src/stl.hpp:18-83 parses (one leading blank on vertex lines)."""
+    """ASCII STL in the layout src/stl.hpp:18-83 parses (one leading blank on vertex lines).
+    ``tris`` is one (ntri, 3, 3) array, or a list of (name, tris) pairs written as patches."""
+    patches = tris if isinstance(tris, list) else [(name, tris)]
     with open(path, "w") as fh:
-        fh.write(f"solid {name}\n")
-        for t in tris:
-            n = np.cross(t[1] - t[0], t[2] - t[0])
-            ln = np.linalg.norm(n)
-            n = n / ln if ln > 0 else n
-            fh.write(f"  facet normal {n[0]:.6e} {n[1]:.6e} {n[2]:.6e}\n    outer loop\n")
-            for v in t:
-                fh.write(f"      vertex {v[0]:.6e} {v[1]:.6e} {v[2]:.6e}\n")
-            fh.write("    endloop\n  endfacet\n")
-        fh.write(f"endsolid {name}\n")
+        for pname, ptris in patches:
+            fh.write(f"solid {pname}\n")
+            for t in ptris:
+                n = np.cross(t[1] - t[0], t[2] - t[0])
+                ln = np.linalg.norm(n)
+                n = n / ln if ln > 0 else n
+                fh.write(f"  facet normal {n[0]:.6e} {n[1]:.6e} {n[2]:.6e}\n    outer loop\n")
+                for v in t:
+                    fh.write(f"      vertex {v[0]:.6e} {v[1]:.6e} {v[2]:.6e}\n")
+                fh.write("    endloop\n  endfacet\n")
+            fh.write(f"endsolid {pname}\n")
+
+
+def _stof(tok):
+    """The float32 nearest to the decimal text (ties to even), as std::stof rounds it."""
+    x = Fraction(tok)
+    f = np.float32(float(x))
+    cands = (np.nextafter(f, np.float32(-np.inf)), f, np.nextafter(f, np.float32(np.inf)))
+    return min(cands, key=lambda c: (abs(Fraction(float(c)) - x), int(np.float32(c).view(np.uint32)) & 1))
+
+
+def read_ascii_stl(path, L=1.0):
+    """Triangles of an ASCII STL as src/stl.hpp:455-523 reads them: the tokens of readToLines
+    (src/input.hpp:90-110, each line split at runs of blanks, so an indented line starts with an
+    empty token), the facets assigned to patches as stl.hpp assigns them, std::stof of each number, vertices divided by L (normalizeSTLv).  Returns (vertices
+    (ntri, 3, 3) float32, normals (ntri, 3) float32, triangles per patch)."""
+    with open(path, newline="\n") as fh:
+        lines = fh.read().split("\n")
+    if lines and lines[-1] == "":  # std::getline yields no line after the final newline
+        lines.pop()
+    toks = [t for line in lines for t in re.split(r"\s+", line)]
+    # one patch per "solid" token (stl.hpp:477-483); facets go to the current patch, which advances
+    # at a "solid" token naming another patch (stl.hpp:486-495)
+    names = [toks[i + 1] if i + 1 < len(toks) else "" for i, t in enumerate(toks) if t == "solid"]
+    counts, verts, norms = [0] * len(names), [], []
+    cur = 0
+    i = 0
+    while i < len(toks):
+        t = toks[i]
+        if t == "solid":
+            if toks[i + 1] != names[cur]:
+                cur += 1
+                i += 1
+        elif t == "facet":
+            norms.append([_stof(toks[i + 2]), _stof(toks[i + 3]), _stof(toks[i + 4])])
+            i += 4
+        elif t == "vertex":
+            tri = []
+            for _ in range(3):
+                tri.append([_stof(toks[i + 1]), _stof(toks[i + 2]), _stof(toks[i + 3])])
+                i += 5
+            i -= 2
+            verts.append(tri)
+            counts[cur] += 1
+        i += 1
+    v = np.array(verts, dtype=np.float32).reshape(-1, 3, 3) / np.float32(L)
+    n = np.array(norms, dtype=np.float32).reshape(-1, 3)
+    return v.astype(np.float32), n, counts
 
 
 def cylinder_markers(n, cx, cy, cz, radius):

@@ -58,7 +58,14 @@ VOXEL_CASES = {
                           lambda: G.ellipsoid_mesh(23, 40, 80, (47.7, 39.2, 35.6), (30.0, 22.0, 20.5), noise=0.05)),
     "ellipsoid_inv_q19": (19, 40, 32, 30, lambda: G.ellipsoid_mesh(31, 18, 36, (19.1, 15.9, 14.6), (13.0, 10.0, 9.0)),
                           1),
+    # two STL patches (setSDF runs once per patch) and bounce-back codes on other faces
+    "two_patch_q19": (19, 36, 28, 26, lambda: [("front", G.ellipsoid_mesh(41, 12, 24, (11.2, 13.7, 12.9), (6.0, 5.0, 5.5))),
+                                               ("back", G.ellipsoid_mesh(43, 12, 24, (24.6, 14.1, 13.3), (5.5, 6.5, 5.0)))],
+                      0, (0, 1, 1, 0, 1, 1)),
 }
+
+# face BC codes (x min, x max, y min, y max, z min, z max) of the voxel cases unless given
+VOXEL_BC = (1, 1, 1, 1, 0, 0)
 
 
 def voxels():
@@ -67,17 +74,19 @@ def voxels():
         for name, spec in VOXEL_CASES.items():
             q, nx, ny, nz, mesh = spec[:5]
             invert = spec[5] if len(spec) > 5 else 0
+            bc = spec[6] if len(spec) > 6 else VOXEL_BC
             stl = os.path.join(td, "walls.stl")
             G.write_ascii_stl(stl, mesh())
             pre = os.path.join(td, "v_")
-            # faces: x BounceBack, y BounceBack, z Cyclic (setSDFnearBwalls sees code 1 on x/y)
+            # face codes as setSDFnearBwalls sees them (1 = BounceBack); withSDF on
             subprocess.run([os.path.join(REF, f"voxel_ref{q}"), stl, str(nx), str(ny), str(nz), "1.0", str(invert),
-                            "1", "1", "1", "1", "1", "0", "0", pre], check=True, stdout=subprocess.DEVNULL)
+                            "1"] + [str(b) for b in bc] + [pre], check=True, stdout=subprocess.DEVNULL)
             out[f"{name}__solid"] = np.fromfile(pre + "solid.u8", dtype=np.uint8)
             out[f"{name}__nei_solid"] = np.fromfile(pre + "neiSolid.u8", dtype=np.uint8)
             out[f"{name}__sdf"] = np.fromfile(pre + "sdf.f32", dtype=np.float32)
             out[f"{name}__shape"] = np.array([q, nx, ny, nz])
             out[f"{name}__invert"] = np.array([invert])
+            out[f"{name}__bc"] = np.array(bc)
             print(name, int(out[f"{name}__solid"].sum()), "solid cells,", int(out[f"{name}__nei_solid"].sum()),
                   "neiSolid cells")
     np.savez_compressed(os.path.join(HERE, "setup_voxels.npz"), **out)
