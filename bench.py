@@ -132,6 +132,23 @@ def make_workload(name):
         c.u0[inlet] *= (1.0 + rng.uniform(-0.01, 0.01, int(inlet.sum()))).astype(np.float32)
         c.f = None
         return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=64.0 / nx, rest=True)
+    if name == "bluff1024_q27":
+        # bluff body from a seeded procedural STL: a closed ellipsoid mesh of 20,000 triangles with
+        # 5 % radial noise, 400 cells long, in a 1024x384x384 D3Q27 channel (inlet 0.05, Geier outlet,
+        # free-slip y faces, periodic z), nu 1e-5, LES Cs 0.1, IBB on the STL links; voxelised and
+        # given its wall distance on the device.  Upstream IBM cylinder: D = 32, 512 markers (16
+        # rings of 32), sinusoidal y motion of amplitude 16 cells and period 4000 steps.
+        nx, ny, nz = 1024, 384, 384
+        nu = 1e-5
+        faces = K.channel_faces(0.05)
+        boundary, b1, b2, b3, u0, v0, w0 = K.face_arrays(nx, ny, nz, faces)
+        omega = np.full(nx * ny * nz, K.omega_from_nu(nu), np.float32)
+        c = K.Case(nx, ny, nz, 27, dict(faces), boundary, b1, b2, b3, u0, v0, w0, None, None, None, omega, None, nu)
+        tris = G.ellipsoid_mesh(2025, 51, 200, (560.0, 192.0, 192.0), (200.0, 60.0, 60.0), noise=0.05)
+        markers = np.concatenate([G.cylinder_markers(32, 160.0, 192.0, 184.0 + z, 16.0) for z in range(16)])
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, rest=True,
+                       stl=(tris.astype(np.float32), G.facet_normals(tris).astype(np.float32)), markers=markers,
+                       motion=dict(amp=(0.0, 16.0, 0.0), period=4000.0))
     raise KeyError(name)
 
 
@@ -260,7 +277,10 @@ def describe(name, storage):
             "cavity256_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256^3 (synthetic)",
             "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)",
             "step768_q27": f"backward-facing step D3Q27 RR IBB LES {storage.upper()} 768x192x192, step 64, Re 5500, "
-                           "sponge 64 cells (synthetic)"}[name]
+                           "sponge 64 cells (synthetic)",
+            "bluff1024_q27": f"bluff body D3Q27 RR IBB LES {storage.upper()} 1024x384x384, 20,000-triangle noisy "
+                             "ellipsoid (400 cells) voxelised on the device, IBM cylinder D=32 with 512 markers "
+                             "(synthetic)"}[name]
 
 
 BULK_KIND = 0  # D3Q19 bulk kernel variant (--bulk-kind)
@@ -277,10 +297,24 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
     if sel.get("rest"):
         for name in ("boundary", "boundary1", "boundary2", "boundary3", "u0", "v0", "w0", "solid", "nei_solid", "sdf",
                      "omega"):
-            lat.upload(name, getattr(c, name))
+            if getattr(c, name) is not None:
+                lat.upload(name, getattr(c, name))
         lat.init_rest()
     else:
         lat.load_case(c)
+    setup = {}
+    if sel.get("stl") is not None:
+        # solid / neiSolid and the LES wall distance from the STL, on the device
+        verts, normals = sel["stl"]
+        t0 = time.perf_counter()
+        lat.voxelize(verts)
+        t1 = time.perf_counter()
+        lat.build_sdf(verts, normals)
+        t2 = time.perf_counter()
+        setup = {"voxelize_s": t1 - t0, "sdf_s": t2 - t1, "triangles": int(verts.shape[0])}
+    if sel.get("markers") is not None:
+        lat.set_markers(sel["markers"])
+        lat.set_motion(**sel.get("motion", {}))
     spz = sel.get("spz", 0.1)
     stream = torch.cuda.ExternalStream(lat.stream(), device=device)
     lat.step(warmup, les=sel["les"], spz_width=spz, store_fields=0)
@@ -300,14 +334,17 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
     counts = lat.cell_counts()
     out = {"ms_per_step": ms / steps, "cells": c.elements, "fluid": counts["fluid"], "special": counts["special"],
            # k_halo (ghost layer) + k_bulk every step, k_special when the case has special cells
-           "launches_per_step": 3 if counts["special"] > 0 else 2, "lat": lat, "case": c, "sel": sel}
+           "launches_per_step": (3 if counts["special"] > 0 else 2) + (4 if sel.get("markers") is not None else 0),
+           "lat": lat, "case": c, "sel": sel, "setup": setup}
     if timing_pass:
         lat.set_timing(True)
         lat.step(steps, les=sel["les"], spz_width=spz, store_fields=0)
         bulk_ms, n = lat.kernel_time("bulk")
         sp_ms, nsp = lat.kernel_time("special")
         h_ms, nh = lat.kernel_time("halo")
+        i_ms, ni = lat.kernel_time("ibm")
         lat.set_timing(False)
+        out["ibm_ms"] = i_ms / max(ni, 1)
         out["bulk_ms"] = bulk_ms / max(n, 1)
         out["special_ms"] = sp_ms / max(nsp, 1)
         out["halo_ms"] = h_ms / max(nh, 1)
@@ -474,10 +511,10 @@ def main():
     if rank == 0 and not args.no_variants and args.workload == "cavity256":
         for vname, vst in (("cavity256", "fp16s"), ("cavity256", "bf16s"), ("cavity256_q27", "fp32"),
                            ("cavity256_q27", "fp16s"), ("cylinder1024", "fp32"), ("cylinder1024", "fp16s"),
-                           ("step768_q27", "fp32"), ("step768_q27", "fp16s")):
+                           ("step768_q27", "fp32"), ("step768_q27", "fp16s"), ("bluff1024_q27", "fp16s")):
             try:
-                r = run_device(vname, vst, min(args.steps, 50) if vname == "step768_q27" else args.steps,
-                               args.warmup, device)
+                big = vname in ("step768_q27", "bluff1024_q27")
+                r = run_device(vname, vst, min(args.steps, 50) if big else args.steps, args.warmup, device)
                 vq = r["case"].q
                 vb = BYTES_PER_CELL[(vq, vst)]
                 vn = r["fluid"] - r["special"]
@@ -488,6 +525,10 @@ def main():
                     "bulk_GBps": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9,
                     "bulk_frac_of_peak": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9 / peak,
                     "bytes_per_cell": vb}
+                if r["setup"]:
+                    variants[f"{vname}_{vst}"]["setup"] = r["setup"]
+                    variants[f"{vname}_{vst}"]["ibm_ms"] = r.get("ibm_ms")
+                    variants[f"{vname}_{vst}"]["wall_force"] = [float(x) for x in r["lat"].force_sum()]
                 r["lat"].close()
                 del r
             except Exception as ex:  # a failing variant must not hide the headline

@@ -180,11 +180,20 @@ bool admit_one(lbffs_server* s, Request* r)
         r->slot = s->free_slots.back();
         s->free_slots.pop_back();
     }
-    // the slot is in no captured graph (it was freed only after a rebuild dropped its last case)
-    s->h_done[r->slot] = 0;
-    cudaMemcpyAsync(s->d_done + r->slot, s->h_done + r->slot, sizeof(long long), cudaMemcpyHostToDevice,
-                    s->setup_stream);
-    cudaStreamSynchronize(s->setup_stream);
+    // the slot is in no captured graph (it was freed only after a rebuild dropped its last case).
+    // The counter is cleared on the device: the pinned read-back buffer h_done belongs to the loop
+    // thread, whose asynchronous copy of all counters may be landing in it right now.
+    if (cudaMemsetAsync(s->d_done + r->slot, 0, sizeof(long long), s->setup_stream) != cudaSuccess ||
+        cudaStreamSynchronize(s->setup_stream) != cudaSuccess) {
+        r->err = "step counter reset failed";
+        r->state = LBFFS_CASE_FAILED;
+        lbffs_destroy(c);
+        r->ctx = nullptr;
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->free_slots.push_back(r->slot);
+        r->slot = -1;
+        return true;
+    }
     r->t_admit = now_s();
     r->state = LBFFS_CASE_RUNNING;
     return true;

@@ -70,6 +70,15 @@ def ellipsoid_mesh(seed, n_theta, n_phi, center, radii, noise=0.05):
     return np.array(tris)
 
 
+def facet_normals(tris):
+    """Unit normals (v1 - v0) x (v2 - v0) of (ntri, 3, 3) triangles, in float64 (zero for a
+    degenerate triangle)."""
+    t = np.asarray(tris, dtype=np.float64)
+    n = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+    ln = np.linalg.norm(n, axis=1, keepdims=True)
+    return np.where(ln > 0, n / np.where(ln > 0, ln, 1.0), n)
+
+
 def write_ascii_stl(path, tris, name="walls"):
     """ASCII STL in the layout src/stl.hpp:18-83 parses (one leading blank on vertex lines).
     ``tris`` is one (ntri, 3, 3) array, or a list of (name, tris) pairs written as patches."""
@@ -77,10 +86,7 @@ def write_ascii_stl(path, tris, name="walls"):
     with open(path, "w") as fh:
         for pname, ptris in patches:
             fh.write(f"solid {pname}\n")
-            for t in ptris:
-                n = np.cross(t[1] - t[0], t[2] - t[0])
-                ln = np.linalg.norm(n)
-                n = n / ln if ln > 0 else n
+            for t, n in zip(ptris, facet_normals(ptris)):
                 fh.write(f"  facet normal {n[0]:.6e} {n[1]:.6e} {n[2]:.6e}\n    outer loop\n")
                 for v in t:
                     fh.write(f"      vertex {v[0]:.6e} {v[1]:.6e} {v[2]:.6e}\n")

@@ -145,3 +145,28 @@ def test_serving_workload_sample_matches_plain_lattices(cuda_lib):
             d = max(float(np.abs(a - b).max()) for a, b in zip(served[k], ref))
             bad.append((k, c.nx, c.ny, c.nz, st, steps, wall, d))
     assert not bad, bad
+
+
+def test_slot_reuse_under_continuous_admission(cuda_lib):
+    """Two slots and one step per round, so every round retires a case and admits the next into
+    the slot just freed while the batch of the other slot runs: each served result equals the
+    plain Lattice run of the same case and step count (a reused slot's step counter starts at 0)."""
+    import lbffs_gb300 as L
+    from lbffs_gb300.serve import Server
+    rng = np.random.default_rng(11)
+    base = [_cavity(12, 0.05, 0.02), _cavity(14, 0.04, 0.03)]
+    runs = [(int(rng.integers(0, 2)), int(rng.integers(2, 14)), "fp32" if k % 3 else "fp16s") for k in range(24)]
+    with Server(hbm_budget=1 << 28, max_cases=2, steps_per_round=1) as srv:
+        ids = []
+        for b, steps, st in runs:
+            ids.append(srv.submit(base[b], steps, storage=st))
+            time.sleep(float(rng.uniform(0.0, 0.002)))
+        for cid in ids:
+            srv.wait(cid)
+        served = [_served_fields(srv, cid) for cid in ids]
+    want = {}
+    for b, steps, st in runs:
+        if (b, steps, st) not in want:
+            want[(b, steps, st)] = _lattice_fields(base[b], steps, st, "bb")
+    bad = [k for k, r in enumerate(runs) if not _same(served[k], want[r])]
+    assert not bad, bad
