@@ -12,14 +12,17 @@ struct BatchCase {
     StepArgs args[2];  // args[p]: source populations and macroscopics are copy p
     long long nsteps;  // steps the case runs in total
     int slot;          // index of the case's step counter
-    int tiles_x;       // bulk tiles per row: ceil(nx / (BULK_BX * BULK_V))
-    int tiles;         // bulk tiles of the case
+    int seg_per_row;   // 32-cell x segments per row: ceil(nx / 32)
+    int tiles;         // bulk tiles of the case: ceil(seg_per_row * ny * nz / BATCH_SEG_PER_TILE)
 };
 
+// x segments one bulk tile covers (BULK_V per warp of a BULK_BX-thread CTA; bulk_segments)
+constexpr int BATCH_SEG_PER_TILE = (BULK_BX / 32) * BULK_V;
 // bulk tiles one CTA of the batched kernel runs (one case's argument copy serves them all)
 constexpr int BATCH_TILES_PER_CTA = 8;
 
-// Bulk step of every case in cases[0..ncases): CTA b runs run b - tile_start[c] of the case c
+// Bulk step of every case in cases[0..ncases), in the segment mapping of bulk_segments (narrow
+// rows keep the lanes busy): CTA b runs run b - tile_start[c] of the case c
 // with tile_start[c] <= b < tile_start[c + 1] (prefix sums of runs of BATCH_TILES_PER_CTA tiles;
 // ntiles = tile_start[ncases] CTAs).
 cudaError_t batch_bulk(int storage, bool les, const BatchCase* cases, const int* tile_start, int ncases, int ntiles,

@@ -29,7 +29,7 @@ __device__ __forceinline__ int find_case(const T* __restrict__ start, int n, T k
 }
 
 template <bool LES>
-__global__ void __launch_bounds__(BULK_BX) k_bulk_batch(const BatchCase* __restrict__ cases,
+__global__ void __launch_bounds__(BULK_BX, 8) k_bulk_batch(const BatchCase* __restrict__ cases,
                                                         const int* __restrict__ tile_start, int ncases,
                                                         const long long* __restrict__ done)
 {
@@ -51,12 +51,11 @@ __global__ void __launch_bounds__(BULK_BX) k_bulk_batch(const BatchCase* __restr
     if (threadIdx.x == 0 && s_last) sa.store_all = 1;  // full macroscopic fields on the final step
     __syncthreads();
     const int run = (int)blockIdx.x - tile_start[s_case];
-    const int tx = cases[s_case].tiles_x, tiles = cases[s_case].tiles;
+    const int spr = cases[s_case].seg_per_row, tiles = cases[s_case].tiles;
+    const int nseg = spr * sa.ny * sa.nz;
     const int t1 = min(tiles, (run + 1) * BATCH_TILES_PER_CTA);
-    for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++) {
-        const int xb = tile % tx, row = tile / tx;
-        bulk_block<19, S, COLL_RR, SGS_SMAG, LES>(sa, xb, row % sa.ny, row / sa.ny);
-    }
+    for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++)
+        bulk_segments<19, S, COLL_RR, SGS_SMAG, LES>(sa, tile * BATCH_SEG_PER_TILE, spr, nseg);
 }
 
 __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* __restrict__ cases,

@@ -281,8 +281,9 @@ cudaError_t build_batch(lbffs_server* s)
             for (int p = 0; p < 2; p++) ctx_step_args(c, &r->params, p, p, hc[i].args[p]);
             hc[i].nsteps = r->nsteps;
             hc[i].slot = r->slot;
-            hc[i].tiles_x = (c->d.nx + BULK_BX * BULK_V - 1) / (BULK_BX * BULK_V);
-            hc[i].tiles = hc[i].tiles_x * c->d.ny * c->d.nz;
+            hc[i].seg_per_row = (c->d.nx + 31) / 32;
+            hc[i].tiles = (int)(((long long)hc[i].seg_per_row * c->d.ny * c->d.nz + BATCH_SEG_PER_TILE - 1) /
+                                BATCH_SEG_PER_TILE);
             tiles[i + 1] = tiles[i] + (hc[i].tiles + BATCH_TILES_PER_CTA - 1) / BATCH_TILES_PER_CTA;
             sp[i + 1] = sp[i] + c->n_special;
             hl[i + 1] = hl[i] + halo_blocks(c->pg, 19, 0) + halo_blocks(c->pg, 19, 1) + halo_blocks(c->pg, 19, 2);

@@ -319,6 +319,51 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     }
 }
 
+// Segment mapping of the same per-cell work, for lattices with narrow rows: a row is cut into
+// ceil(nx / 32) segments of 32 cells, segments are numbered row after row ((j, k) order), and warp
+// w of the CTA takes segments g0 + BULK_V * w + v.  A 24-cell row then keeps 24 of 32 lanes busy
+// where a BULK_BX * BULK_V-cell row tile keeps 24 of 256.  spr = segments per row, nseg = all.
+template <int Q, int S, int COLL, int SGS, bool LES>
+__device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr, int nseg)
+{
+    using T = typename Codec<S>::T;
+    constexpr bool HELD = (Q == 19);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int ci[BULK_V], cj[BULK_V], ck[BULK_V];
+    uint8_t fl[BULK_V];
+    bool act[BULK_V];
+    bool any = false;
+#pragma unroll
+    for (int v = 0; v < BULK_V; v++) {
+        const int g = g0 + warp * BULK_V + v;
+        const int row = g / spr;
+        ci[v] = (g - row * spr) * 32 + lane;
+        cj[v] = row % a.ny;
+        ck[v] = row / a.ny;
+        fl[v] = (g < nseg && ci[v] < a.nx) ? __ldg(a.flags + (long long)row * a.nx + ci[v]) : FL_SOLID;
+        act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
+        any |= act[v];
+    }
+    if (!any) return;
+    float ft[BULK_V][Q];
+#pragma unroll
+    for (int v = 0; v < BULK_V; v++) {
+        if (!act[v]) continue;
+        const int ip = pidx(a, ci[v], cj[v], ck[v]);
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
+            ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < BULK_V; v++) {
+        if (!act[v]) continue;
+        const int ic = (ck[v] * a.ny + cj[v]) * a.nx + ci[v];
+        bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], ci[v], cj[v], ck[v], ic, pidx(a, ci[v], cj[v], ck[v]));
+    }
+}
+
 template <int Q, int S, int COLL, int SGS, bool LES>
 __global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
 {
