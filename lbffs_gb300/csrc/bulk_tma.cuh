@@ -193,9 +193,23 @@ __global__ void __launch_bounds__(TMA_TW) k_bulk_tma(const StepArgs a, long long
         if (act) {
             const T* row = in + st * 19 * L::ROW + L::E16 + tid;
             float ft[19];
+            if constexpr (SGS != SGS_WALE) {
+                // the two-lane collision of the per-thread kernel with the second lane idle, so
+                // both variants round every cell the same way
+                F2 fp[19];
 #pragma unroll
-            for (int q = 0; q < 19; q++) ft[q] = held_of(row[q * L::ROW - lat_c(19, q, 0)]);
-            bulk_collide<19, S, COLL_RR, SGS, LES>(a, ft, fl, i, j, k, ic);
+                for (int q = 0; q < 19; q++) fp[q] = pk(held_of(row[q * L::ROW - lat_c(19, q, 0)]), 0.f);
+                const uint8_t fl2[2] = {fl, FL_SOLID};
+                const bool act2[2] = {true, false};
+                const int ci[2] = {i, i}, cj[2] = {j, j}, ck[2] = {k, k}, ic2[2] = {ic, ic};
+                bulk_collide2<S, LES>(a, fp, fl2, act2, ci, cj, ck, ic2);
+#pragma unroll
+                for (int q = 0; q < 19; q++) ft[q] = lane0(fp[q]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 19; q++) ft[q] = held_of(row[q * L::ROW - lat_c(19, q, 0)]);
+                bulk_collide<19, S, COLL_RR, SGS, LES>(a, ft, fl, i, j, k, ic);
+            }
             if (clean) {
                 T* o = out + st * 19 * TMA_TW + tid;
 #pragma unroll

@@ -14,6 +14,7 @@
 //                   fifth-order back-conversion products.
 #pragma once
 #include "lbffs_common.cuh"
+#include "pair.cuh"
 
 namespace lbffs {
 
@@ -111,28 +112,37 @@ __device__ __forceinline__ void collide_rr19(float (&f)[19], float rho, const fl
 // rho - 1, so both forms share it and the large constant parts never cancel in FP32.
 // Moments of the held values.  With a held scale HS (2^15 for FP16S storage) r, j and s are HS
 // times the moments of f (f form) or of f - w (deviation form); rho is unscaled.
-struct Mom19 {
-    float r;        // sum of the held values: rho (f form) or rho - 1 (deviation form)
-    float rho;
-    float j[3];     // sum_q c_q f_q
-    float s[3][3];  // sum_q c_a c_b (held value); diagonal: sum c_a^2 f_q - 1/3 in deviation form
+// The value type V is float (one cell) or F2 (two cells in packed FP32x2 lanes); the expressions
+// are the same for both.
+template <class V>
+struct Mom19T {
+    V r;        // sum of the held values: rho (f form) or rho - 1 (deviation form)
+    V rho;
+    V j[3];     // sum_q c_q f_q
+    V s[3][3];  // sum_q c_a c_b (held value); diagonal: sum c_a^2 f_q - 1/3 in deviation form
 };
+using Mom19 = Mom19T<float>;
 
-template <bool DEV, int HS = 1>
-__device__ __forceinline__ Mom19 moments19(const float (&f)[19])
+template <bool DEV, int HS = 1, class V = float>
+__device__ __forceinline__ Mom19T<V> moments19(const V (&f)[19])
 {
-    const float a1 = f[1] + f[2], d1 = f[1] - f[2], a3 = f[3] + f[4], d3 = f[3] - f[4];
-    const float a5 = f[5] + f[6], d5 = f[5] - f[6], a7 = f[7] + f[8], d7 = f[7] - f[8];
-    const float a9 = f[9] + f[10], d9 = f[9] - f[10], a11 = f[11] + f[12], d11 = f[11] - f[12];
-    const float a13 = f[13] + f[14], d13 = f[13] - f[14], a15 = f[15] + f[16], d15 = f[15] - f[16];
-    const float a17 = f[17] + f[18], d17 = f[17] - f[18];
-    Mom19 m;
+    const V a1 = f[1] + f[2], d1 = f[1] - f[2], a3 = f[3] + f[4], d3 = f[3] - f[4];
+    const V a5 = f[5] + f[6], d5 = f[5] - f[6], a7 = f[7] + f[8], d7 = f[7] - f[8];
+    const V a9 = f[9] + f[10], d9 = f[9] - f[10], a11 = f[11] + f[12], d11 = f[11] - f[12];
+    const V a13 = f[13] + f[14], d13 = f[13] - f[14], a15 = f[15] + f[16], d15 = f[15] - f[16];
+    const V a17 = f[17] + f[18], d17 = f[17] - f[18];
+    Mom19T<V> m;
     m.s[0][0] = (a1 + a7) + (a9 + a11) + a13;
     m.s[1][1] = (a3 + a7) + (a9 + a15) + a17;
     m.s[2][2] = (a5 + a11) + (a13 + a15) + a17;
     m.r = (f[0] + a1) + (a3 + a5) + ((a7 + a9) + (a11 + a13)) + (a15 + a17);
-    if constexpr (HS == 1) m.rho = DEV ? 1.f + m.r : m.r;
-    else m.rho = DEV ? 1.f + m.r * (1.f / HS) : m.r * (1.f / HS);
+    if constexpr (HS == 1) {
+        if constexpr (DEV) m.rho = 1.f + m.r;
+        else m.rho = m.r;
+    } else {
+        if constexpr (DEV) m.rho = 1.f + m.r * (1.f / HS);
+        else m.rho = m.r * (1.f / HS);
+    }
     m.j[0] = (d1 + d7) + (d9 + d11) + d13;
     m.j[1] = (d3 + d7) - d9 + (d15 + d17);
     m.j[2] = (d5 + d11) - d13 + (d15 - d17);
@@ -142,16 +152,15 @@ __device__ __forceinline__ Mom19 moments19(const float (&f)[19])
     return m;
 }
 
-// smagorinskyTauSGS without damping, with sum_q c_a c_b feq_q = rho delta_ab / 3 + u_a u_b for the
-// reference's feq = (rho + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) w_q (fourth-order isotropy of D3Q19);
-// s_aa - r/3 is sum c_a^2 f - rho/3 in either form
-template <int HS = 1>
-__device__ __forceinline__ float smagorinsky19(const Mom19& m, float u, float v, float w, float omega, float les,
-                                               float cs)
+// sum over the components of the non-equilibrium stress squared, Pi_neq : Pi_neq, of
+// smagorinskyTauSGS, with sum_q c_a c_b feq_q = rho delta_ab / 3 + u_a u_b for the reference's
+// feq = (rho + 3 c.u + 4.5 (c.u)^2 - 1.5 u^2) w_q (fourth-order isotropy of D3Q19); s_aa - r/3 is
+// sum c_a^2 f - rho/3 in either form
+template <int HS = 1, class V = float>
+__device__ __forceinline__ V smag_pp19(const Mom19T<V>& m, V u, V v, V w)
 {
-    const float tau = 1.f / omega;
-    const float r3 = m.r * (1.f / 3.f);
-    float pxx, pyy, pzz, pxy, pxz, pyz;
+    const V r3 = m.r * (1.f / 3.f);
+    V pxx, pyy, pzz, pxy, pxz, pyz;
     if constexpr (HS == 1) {
         pxx = m.s[0][0] - r3 - u * u, pyy = m.s[1][1] - r3 - v * v, pzz = m.s[2][2] - r3 - w * w;
         pxy = m.s[0][1] - u * v, pxz = m.s[0][2] - u * w, pyz = m.s[1][2] - v * w;
@@ -160,31 +169,46 @@ __device__ __forceinline__ float smagorinsky19(const Mom19& m, float u, float v,
         pxx = (m.s[0][0] - r3) * is - u * u, pyy = (m.s[1][1] - r3) * is - v * v, pzz = (m.s[2][2] - r3) * is - w * w;
         pxy = m.s[0][1] * is - u * v, pxz = m.s[0][2] * is - u * w, pyz = m.s[1][2] * is - v * w;
     }
-    const float pp = pxx * pxx + pyy * pyy + pzz * pzz + 2.f * (pxy * pxy + pxz * pxz + pyz * pyz);
-    return les * 0.5f * (-tau + sqrtf(tau * tau + 18.f * 1.41421356237f * cs * cs * sqrtf(pp) / m.rho));
+    return pxx * pxx + pyy * pyy + pzz * pzz + 2.f * (pxy * pxy + pxz * pxz + pyz * pyz);
+}
+
+// the eddy relaxation time of smagorinskyTauSGS (without damping) from Pi_neq : Pi_neq
+__device__ __forceinline__ float smag_tau(float pp, float rho, float omega, float les, float cs)
+{
+    const float tau = 1.f / omega;
+    return les * 0.5f * (-tau + sqrtf(tau * tau + 18.f * 1.41421356237f * cs * cs * sqrtf(pp) / rho));
+}
+
+template <int HS = 1>
+__device__ __forceinline__ float smagorinsky19(const Mom19& m, float u, float v, float w, float omega, float les,
+                                               float cs)
+{
+    return smag_tau(smag_pp19<HS>(m, u, v, w), m.rho, omega, les, cs);
 }
 
 // recursive regularised collision (D3Q19 kernel.cl:3156-3309) from the moments; U without the half-force
 // shift.  Each output is written w_q * r + rho * (deviation), i.e. f_q or f_q - w_q as held, times the
 // held scale HS (a power of two, so the scaled results are the unscaled ones times HS exactly).
-template <int HS = 1>
-__device__ __forceinline__ void collide_rr19m(float (&f)[19], const Mom19& m, const float (&U)[3], float we,
+// ir1 = 1 / rho (one division per cell, computed by the caller).
+template <int HS = 1, class V = float>
+__device__ __forceinline__ void collide_rr19m(V (&f)[19], const Mom19T<V>& m, const V (&U)[3], V we, V ir1,
                                               float omega_b, float dpdx)
 {
-    const float third = 1.f / 3.f, k1 = 1.f - we, rho = m.rho;
-    const float ir = (1.f / rho) * (1.f / HS);
-    const float r3 = m.r * third;
-    float N2[3][3], R2[3][3];
+    const float third = 1.f / 3.f;
+    const V k1 = 1.f - we, rho = m.rho;
+    const V ir = ir1 * (1.f / HS);
+    const V r3 = m.r * third;
+    V N2[3][3], R2[3][3];
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = a; b < 3; b++) {
-            const float m2 = (a == b) ? (m.s[a][a] - r3) * ir : m.s[a][b] * ir;
+            const V m2 = (a == b) ? (m.s[a][a] - r3) * ir : m.s[a][b] * ir;
             N2[a][b] = N2[b][a] = m2 - U[a] * U[b];
             R2[a][b] = R2[b][a] = m2;
         }
-    const float wm = (omega_b - we) * third;
-    const float nsum = N2[0][0] + N2[1][1] + N2[2][2];
+    const V wm = (omega_b - we) * third;
+    const V nsum = N2[0][0] + N2[1][1] + N2[2][2];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         R2[a][a] -= wm * nsum + we * N2[a][a];  // omega_P on the own axis, omega_M on the others
@@ -192,7 +216,7 @@ __device__ __forceinline__ void collide_rr19m(float (&f)[19], const Mom19& m, co
         for (int b = a + 1; b < 3; b++) R2[a][b] = R2[b][a] = R2[a][b] - we * N2[a][b];
     }
     // T3[a][b]: c_a^2 c_b moment; Q4[a][b]: c_a^2 c_b^2 moment minus its constant 1/9
-    float T3[3][3], Q4[3][3];
+    V T3[3][3], Q4[3][3];
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll
@@ -200,34 +224,44 @@ __device__ __forceinline__ void collide_rr19m(float (&f)[19], const Mom19& m, co
             if (a == b) continue;
             T3[a][b] = U[a] * U[a] * U[b] + k1 * (U[b] * N2[a][a] + 2.f * U[a] * N2[a][b]) + third * U[b];
             if (b > a) {
-                const float n4 = U[b] * U[b] * N2[a][a] + U[a] * U[a] * N2[b][b] + 4.f * U[a] * U[b] * N2[a][b];
+                const V n4 = U[b] * U[b] * N2[a][a] + U[a] * U[a] * N2[b][b] + 4.f * U[a] * U[b] * N2[a][b];
                 Q4[a][b] = Q4[b][a] = U[a] * U[a] * U[b] * U[b] + k1 * n4 + third * (R2[a][a] + R2[b][b]);
             }
         }
-    const float h = rho * (0.5f * HS), qr = rho * (0.25f * HS);
-    const float base1 = m.r * (1.f / 18.f), base2 = m.r * (1.f / 36.f);
-    const float src1 = rho * 3.f * dpdx * (1.f / 18.f) * HS, src2 = rho * 3.f * dpdx * (1.f / 36.f) * HS;
+    const V h = rho * (0.5f * HS), qr = rho * (0.25f * HS);
+    const V base1 = m.r * (1.f / 18.f), base2 = m.r * (1.f / 36.f);
+    const V src1 = rho * (3.f * dpdx * (1.f / 18.f) * HS), src2 = rho * (3.f * dpdx * (1.f / 36.f) * HS);
     // axis pairs (q+, q-) = (1,2) (3,4) (5,6)
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const int b = (a + 1) % 3, d = (a + 2) % 3;
-        const float A = base1 + h * (R2[a][a] - Q4[a][b] - Q4[a][d]);
-        const float B = h * (U[a] - T3[b][a] - T3[d][a]);
-        const float s = (a == 0) ? src1 : 0.f;
-        f[1 + 2 * a] = A + B + s;
-        f[2 + 2 * a] = A - B - s;
+        const V A = base1 + h * (R2[a][a] - Q4[a][b] - Q4[a][d]);
+        const V B = h * (U[a] - T3[b][a] - T3[d][a]);
+        if (a == 0) {
+            f[1] = A + B + src1;
+            f[2] = A - B - src1;
+        } else {
+            f[1 + 2 * a] = A + B;
+            f[2 + 2 * a] = A - B;
+        }
     }
     // diagonal planes (a,b) = (x,y) q7-10, (x,z) q11-14, (y,z) q15-18: (+,+) (-,-) (+,-) (-,+)
 #pragma unroll
     for (int p = 0; p < 3; p++) {
         const int a = p < 2 ? 0 : 1, b = p == 0 ? 1 : 2;
-        const float P = base2 + qr * Q4[a][b], Rr = qr * R2[a][b], X = qr * T3[a][b], Y = qr * T3[b][a];
-        const float pp = P + Rr, pm = P - Rr, xp = X + Y, xm = Y - X;
-        const float s = (a == 0) ? src2 : 0.f;
-        f[7 + 4 * p] = pp + xp + s;
-        f[8 + 4 * p] = pp - xp - s;
-        f[9 + 4 * p] = pm + xm + s;
-        f[10 + 4 * p] = pm - xm - s;
+        const V P = base2 + qr * Q4[a][b], Rr = qr * R2[a][b], X = qr * T3[a][b], Y = qr * T3[b][a];
+        const V pp = P + Rr, pm = P - Rr, xp = X + Y, xm = Y - X;
+        if (a == 0) {
+            f[7 + 4 * p] = pp + xp + src2;
+            f[8 + 4 * p] = pp - xp - src2;
+            f[9 + 4 * p] = pm + xm + src2;
+            f[10 + 4 * p] = pm - xm - src2;
+        } else {
+            f[7 + 4 * p] = pp + xp;
+            f[8 + 4 * p] = pp - xp;
+            f[9 + 4 * p] = pm + xm;
+            f[10 + 4 * p] = pm - xm;
+        }
     }
     // rest population last: it absorbs the rounding of the other 18, so each cell's mass is kept to
     // within one unbiased rounding (the collision conserves mass exactly in real arithmetic)

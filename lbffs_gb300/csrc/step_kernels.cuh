@@ -235,7 +235,7 @@ __device__ __forceinline__ void bulk_collide(const StepArgs& a, float (&ft)[Q], 
             a.tau_n[ic] = tsgs;
         }
         const float U[3] = {u - 0.5f * a.dpdx * ir, v, w};
-        collide_rr19m<HS>(ft, m, U, we, a.omega_b, a.dpdx);
+        collide_rr19m<HS>(ft, m, U, we, ir, a.omega_b, a.dpdx);
     } else {
         macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
         if constexpr (SGS == SGS_WALE) {
@@ -275,6 +275,79 @@ __device__ __forceinline__ void bulk_cell(const StepArgs& a, float (&ft)[Q], uin
     }
 }
 
+// bulk_collide for the two cells of a thread at once (D3Q19, Smagorinsky or no SGS): the moments,
+// the velocity and the recursive regularised collision run on packed FP32x2 lanes (lane v = cell
+// v); the per-cell parts (relaxation rates, eddy viscosity square roots, sponge, field stores)
+// run per lane.  act[v]: cell v is a bulk cell (the other lane's values are computed and dropped).
+template <int S, bool LES>
+__device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], const uint8_t (&fl)[2],
+                                              const bool (&act)[2], const int (&ci)[2], const int (&cj)[2],
+                                              const int (&ck)[2], const int (&ic)[2])
+{
+    constexpr int HS = Codec<S>::HS;
+    const Mom19T<F2> m = moments19<Codec<S>::DEV, HS>(ft);
+    float irl[2], oml[2];
+#pragma unroll
+    for (int v = 0; v < 2; v++) {
+        oml[v] = (fl[v] & FL_OMEGA) ? __ldg(a.omega + ic[v]) : a.omega0;
+        irl[v] = 1.f / lane(m.rho, v);
+    }
+    const F2 ir = pk(irl[0], irl[1]);
+    const F2 irs = ir * (1.f / HS);
+    const F2 u = m.j[0] * irs + (0.5f * a.dpdx) * ir;  // updateRhoUVW (kernel.cl:3509-3523)
+    const F2 v = m.j[1] * irs;
+    const F2 w = m.j[2] * irs;
+    float tsl[2] = {0.f, 0.f}, wel[2];
+    F2 pp;
+    if constexpr (LES) pp = smag_pp19<HS>(m, u, v, w);
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        const float rho = lane(m.rho, c);
+        if constexpr (LES) {
+            tsl[c] = smag_tau(lane(pp, c), rho, oml[c], a.les, a.cs);
+            if (fl[c] & FL_SDF) tsl[c] = damping(tsl[c], __ldg(a.sdf + ic[c]), a.cs);
+        }
+        if (act[c]) {
+            if (a.err && !(rho == rho)) atomicOr(a.err, 1);
+            if (a.store_all || (fl[c] & FL_STORE) || in_box(a, ci[c], cj[c], ck[c])) {
+                a.rho_n[ic[c]] = rho;
+                a.u_n[ic[c]] = lane(u, c);
+                a.v_n[ic[c]] = lane(v, c);
+                a.w_n[ic[c]] = lane(w, c);
+                a.tau_n[ic[c]] = tsl[c];
+            }
+        }
+        const float tau = sponge_tau(a, 1.f / oml[c], tsl[c], ci[c], cj[c], ck[c]);
+        wel[c] = 1.f / (tau + tsl[c]);
+    }
+    const F2 U[3] = {u - (0.5f * a.dpdx) * ir, v, w};
+    collide_rr19m<HS>(ft, m, U, pk(wel[0], wel[1]), ir, a.omega_b, a.dpdx);
+}
+
+// Two cells of one thread through bulk_collide2, then the stores of the active ones.
+template <int S, bool LES>
+__device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
+                                          const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
+                                          const int (&ic)[2], const int (&ip)[2])
+{
+    using T = typename Codec<S>::T;
+    F2 ft[19];
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        const T* p = static_cast<const T*>(a.fin_s[q]);
+        const float x0 = act[0] ? Codec<S>::load_held(p + ip[0]) : 0.f;
+        const float x1 = act[1] ? Codec<S>::load_held(p + ip[1]) : 0.f;
+        ft[q] = pk(x0, x1);
+    }
+    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic);
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        T* p = static_cast<T*>(a.fout_q[q]);
+        if (act[0]) Codec<S>::store_held(p + ip[0], lane0(ft[q]));
+        if (act[1]) Codec<S>::store_held(p + ip[1], lane1(ft[q]));
+    }
+}
+
 // One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
 // instruction of a warp covers 32 consecutive cells.  Every population is pulled from the same
 // offset for every cell: cells on the domain border read the ghost layer, which k_halo filled
@@ -300,6 +373,12 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         any |= act[v];
     }
     if (!any) return;
+    if constexpr (Q == 19 && SGS != SGS_WALE && BULK_V == 2) {
+        const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
+        const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
+        bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
+        return;
+    }
     float ft[BULK_V][Q];
 #pragma unroll
     for (int v = 0; v < BULK_V; v++) {
@@ -345,6 +424,12 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
         any |= act[v];
     }
     if (!any) return;
+    if constexpr (Q == 19 && SGS != SGS_WALE && BULK_V == 2) {
+        const int ic[2] = {(ck[0] * a.ny + cj[0]) * a.nx + ci[0], (ck[1] * a.ny + cj[1]) * a.nx + ci[1]};
+        const int ip[2] = {pidx(a, ci[0], cj[0], ck[0]), pidx(a, ci[1], cj[1], ck[1])};
+        bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
+        return;
+    }
     float ft[BULK_V][Q];
 #pragma unroll
     for (int v = 0; v < BULK_V; v++) {
@@ -553,7 +638,7 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     const float tau = sponge_tau(a, 1.f / omega, tsgs, x[0], x[1], x[2]);
     if constexpr (Q == 19) {
         const float U[3] = {u - 0.5f * a.dpdx / rho, v, w};
-        collide_rr19m(ft, m19, U, 1.f / (tau + tsgs), a.omega_b, a.dpdx);
+        collide_rr19m(ft, m19, U, 1.f / (tau + tsgs), 1.f / rho, a.omega_b, a.dpdx);
     } else {
         collide<Q, COLL>(ft, rho, u, v, w, 1.f / (tau + tsgs), a);
     }
