@@ -31,7 +31,8 @@ build fails loudly if an anchor is missing):
 
 The host geometry code (``src/walls.hpp`` / ``src/stl.hpp``) is compiled
 by the same recipe into ``voxel_ref19`` / ``voxel_ref27`` with ``boost_stub/`` standing in for
-the one Boost call it uses, and ``src/setBoundaryConditions.hpp`` into ``case_ref``.
+the one Boost call it uses, ``src/setBoundaryConditions.hpp`` into ``case_ref``, and the output
+step ``D3Q<Q>_opencl/write.hpp`` into ``output_ref19`` / ``output_ref27``.
 
 Usage: ``python oracle/build_ref.py [--jobs N]``.  Without the reference
 checkout (e.g. on a machine the tree was copied to) it compiles the patched
@@ -172,6 +173,19 @@ def build_voxel(q, jobs_log):
     return True
 
 
+def build_output(q, jobs_log):
+    exe = os.path.join(OUT, f"output_ref{q}")
+    lat = os.path.join(REF, f"D3Q{q}_opencl")
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-w", f"-DOUT_Q={q}",
+           f"-I{os.path.join(HERE, 'boost_stub')}", f"-I{os.path.join(REF, 'src')}", f"-I{lat}",
+           os.path.join(HERE, "output_driver.cpp"), "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        jobs_log.append(f"output_ref{q}: {r.stderr[-2000:]}")
+        return False
+    return True
+
+
 def build_case(jobs_log):
     exe = os.path.join(OUT, "case_ref")
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-w", f"-I{os.path.join(REF, 'src')}",
@@ -212,6 +226,7 @@ def main(argv=None):
         futs = [ex.submit(build_one, *v, log) for v in variants]
         if have_ref:
             futs += [ex.submit(build_voxel, q, log) for q in (19, 27)]
+            futs += [ex.submit(build_output, q, log) for q in (19, 27)]
             futs.append(ex.submit(build_case, log))
         ok = all(f.result() for f in futs)
     if not ok:
