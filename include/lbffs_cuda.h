@@ -95,7 +95,17 @@ enum lbffs_field {
     LBFFS_GXIBM = 20,    /* float32[E] IBM forcing field (GxIBM_d) */
     LBFFS_GYIBM = 21,
     LBFFS_GZIBM = 22,
-    LBFFS_NFIELDS = 23
+    /* output step (lbffs_output): cal_rhoUVW of every cell at the last output, the host arrays
+       rho / u / v / w of write.hpp:27 (download only; zeros before the first output) */
+    LBFFS_OUT_RHO = 23,
+    LBFFS_OUT_U = 24,
+    LBFFS_OUT_V = 25,
+    LBFFS_OUT_W = 26,
+    /* time-mean accumulators uMean / vMean / wMean of write.hpp:70-76 (upload restores them) */
+    LBFFS_UMEAN = 27,
+    LBFFS_VMEAN = 28,
+    LBFFS_WMEAN = 29,
+    LBFFS_NFIELDS = 30
 };
 
 /* Per-step scalars: the trailing arguments of k_streamingCollision (ns.cpp:528-535). */
@@ -183,6 +193,44 @@ int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
    vertices after normalizeSTLv (stl.hpp:161-175), all patches concatenated.  Replaces the SOLID
    and NEISOLID fields; the geometry takes effect at the next lbffs_step. */
 int lbffs_voxelize(lbffs_ctx* ctx, const float* vertices, long long ntri, int invert);
+
+/* ---- Output step (D3Q19_opencl/write.hpp; D3Q27_opencl/write.hpp differs only in the restart
+   file's population count) ---- */
+typedef struct lbffs_output_params {
+    float dpdx;        /* cal_rhoUVW's half-force shift (the step's dpdx) */
+    float c;           /* velocity scale uMax / U0 of the VTK fields and of uAve */
+    float L;           /* cell size of the VTK SPACING line and of the sdf / nuSGS fields */
+    int out_interval;  /* outInterval: the weight of this output in the time means; 0 leaves them */
+    int force_coeffs;  /* forceCoeffs: sum the wall and IBM forces, write the IBM fields (else zeros) */
+} lbffs_output_params;
+
+typedef struct lbffs_output_result {
+    float rho_av;           /* rho_av_tmp / float(eleFluid) + 1 (write.hpp:47), the sum in FP64 */
+    float rho_max, rho_min; /* over all cells (write.hpp:48-49) */
+    float u_ave;            /* mean of u * c over the x = 0 plane, summed in the reference's float order */
+    float time_mean;        /* timeMean after this output */
+    long long n_fluid;      /* eleFluid */
+    double fw[3];           /* SumFwx.. over fluid cells in FP64 (the reference sums in float) */
+    double g_ibm[3];        /* SumGxIBM.. over fluid cells in FP64 */
+} lbffs_output_result;
+
+/* write.hpp:16-76 on the device: rho / u / v / w of every cell from the current populations by
+   cal_rhoUVW (D3Q19.hpp:647-666, same float order) into LBFFS_OUT_*, the reductions above and, for
+   out_interval > 0, uMean += u * outInterval.  Only the scalars leave the device. */
+int lbffs_output(lbffs_ctx* ctx, const lbffs_output_params* params, lbffs_output_result* out);
+/* The VTK file of write.hpp:78-600 from the last lbffs_output (ASCII, or binary with asciiToBinary's
+   byte order, src/base.hpp:35-43).  Asynchronous: the call queues the device copies behind the work
+   already on the context's stream and returns; a host thread writes the file while later steps
+   run.  lbffs_io_wait (or the next output, upload, voxelisation, SDF or write call) joins it. */
+int lbffs_write_vtk(lbffs_ctx* ctx, const char* path, int binary, const lbffs_output_params* params);
+/* The restart file data.dat of write.hpp:603-631 (int nt, nx, ny, nz; then the populations q-major
+   as float), from the current populations; asynchronous like lbffs_write_vtk (the populations are
+   copied on the device first, so later steps do not change the file). */
+int lbffs_write_restart(lbffs_ctx* ctx, const char* path, int nt);
+/* restart.hpp: a data.dat of this grid into both population copies; *nt = its time step. */
+int lbffs_read_restart(lbffs_ctx* ctx, const char* path, int* nt);
+/* Wait for the asynchronous file write, if any; returns its error. */
+int lbffs_io_wait(lbffs_ctx* ctx);
 
 /* The LES wall-distance set-up of D3Q19_opencl/ns.cpp:200-225 on the device: the SDF field is set
    to sdf_ini, setSDF (src/walls.hpp:218-268, one call per STL patch) runs with (dr, p) around the

@@ -29,7 +29,8 @@ SGS = {"smag": 0, "smagorinsky": 0, "wale": 1}
 WALL = {"bb": 0, "ibb": 1}
 FIELDS = {"f": 0, "boundary": 1, "boundary1": 2, "boundary2": 3, "boundary3": 4, "sdf": 5, "solid": 6,
           "nei_solid": 7, "u0": 8, "v0": 9, "w0": 10, "omega": 11, "tau_sgs": 12, "rho": 13, "u": 14, "v": 15,
-          "w": 16, "fwx": 17, "fwy": 18, "fwz": 19, "gx": 20, "gy": 21, "gz": 22}
+          "w": 16, "fwx": 17, "fwy": 18, "fwz": 19, "gx": 20, "gy": 21, "gz": 22, "out_rho": 23, "out_u": 24,
+          "out_v": 25, "out_w": 26, "u_mean": 27, "v_mean": 28, "w_mean": 29}
 FIELD_DTYPE = {"boundary": np.int32, "boundary1": np.int32, "boundary2": np.int32, "boundary3": np.int32,
                "solid": np.uint8, "nei_solid": np.uint8}
 E_ARG, E_CUDA, E_STATE, E_UNSUPPORTED, E_NONFINITE = -1, -2, -3, -4, -5
@@ -49,6 +50,17 @@ class Desc(C.Structure):
 class StepParams(C.Structure):
     _fields_ = [("dpdx", C.c_float), ("rho_av", C.c_float), ("les", C.c_float), ("omega_b", C.c_float),
                 ("spz_width", C.c_float), ("clim", C.c_float), ("store_fields", C.c_int)]
+
+
+class OutputParams(C.Structure):
+    _fields_ = [("dpdx", C.c_float), ("c", C.c_float), ("L", C.c_float), ("out_interval", C.c_int),
+                ("force_coeffs", C.c_int)]
+
+
+class OutputResult(C.Structure):
+    _fields_ = [("rho_av", C.c_float), ("rho_max", C.c_float), ("rho_min", C.c_float), ("u_ave", C.c_float),
+                ("time_mean", C.c_float), ("n_fluid", C.c_longlong), ("fw", C.c_double * 3),
+                ("g_ibm", C.c_double * 3)]
 
 
 class Motion(C.Structure):
@@ -94,6 +106,11 @@ def load_library():
         "lbffs_init_rest": ([vp], i),
         "lbffs_set_bulk_kernel": ([vp, i], i),
         "lbffs_voxelize": ([vp, C.POINTER(C.c_float), C.c_longlong, i], i),
+        "lbffs_output": ([vp, C.POINTER(OutputParams), C.POINTER(OutputResult)], i),
+        "lbffs_write_vtk": ([vp, C.c_char_p, i, C.POINTER(OutputParams)], i),
+        "lbffs_write_restart": ([vp, C.c_char_p, i], i),
+        "lbffs_read_restart": ([vp, C.c_char_p, C.POINTER(C.c_int)], i),
+        "lbffs_io_wait": ([vp], i),
         "lbffs_build_sdf": ([vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_longlong), i, C.c_float,
                              C.c_float, C.c_float, C.c_float], i),
     }
@@ -199,6 +216,33 @@ class Lattice:
                                              n.ctypes.data_as(C.POINTER(C.c_float)),
                                              pn.ctypes.data_as(C.POINTER(C.c_longlong)), int(pn.size), float(dr),
                                              float(p), float(sdf_ini), float(dr_walls)))
+
+    # ---- output step (write.hpp) ----
+    def output(self, dpdx=0.0, c=1.0, L=1.0, out_interval=0, force_coeffs=False):
+        """rho / u / v / w from the current populations and write.hpp's reductions, on the device;
+        returns the scalars as a dict (the fields: ``download("out_rho")`` ...)."""
+        p = OutputParams(dpdx, c, L, int(out_interval), int(bool(force_coeffs)))
+        r = OutputResult()
+        self._check(self.lib.lbffs_output(self.h, C.byref(p), C.byref(r)))
+        return {"rho_av": r.rho_av, "rho_max": r.rho_max, "rho_min": r.rho_min, "u_ave": r.u_ave,
+                "time_mean": r.time_mean, "n_fluid": r.n_fluid, "fw": list(r.fw), "g_ibm": list(r.g_ibm)}
+
+    def write_vtk(self, path, binary=False, c=1.0, L=1.0, force_coeffs=False):
+        """Queue the VTK file of the last :meth:`output`; returns at once (see :meth:`io_wait`)."""
+        p = OutputParams(0.0, c, L, 0, int(bool(force_coeffs)))
+        self._check(self.lib.lbffs_write_vtk(self.h, os.fsencode(path), int(bool(binary)), C.byref(p)))
+
+    def write_restart(self, path, nt):
+        """Queue the restart file (data.dat layout) of the current populations."""
+        self._check(self.lib.lbffs_write_restart(self.h, os.fsencode(path), int(nt)))
+
+    def read_restart(self, path):
+        nt = C.c_int()
+        self._check(self.lib.lbffs_read_restart(self.h, os.fsencode(path), C.byref(nt)))
+        return nt.value
+
+    def io_wait(self):
+        self._check(self.lib.lbffs_io_wait(self.h))
 
     def set_bulk_kernel(self, kind):
         """D3Q19 bulk kernel variant: 0 per-thread loads, 1 row-staged bulk copies (same results)."""

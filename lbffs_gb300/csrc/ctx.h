@@ -11,6 +11,10 @@
 #include "ibm.h"
 #include "launch.h"
 
+namespace lbffs {
+struct OutputState;  // output.cu: fields of lbffs_output and the asynchronous file writer
+}
+
 struct lbffs_ctx {
     lbffs_desc d{};
     int Q = 19;
@@ -57,6 +61,9 @@ struct lbffs_ctx {
     lbffs::Arena* arena = nullptr;
     bool own_stream = true, own_stage = true;
 
+    // output step and asynchronous writes (output.cu)
+    lbffs::OutputState* out = nullptr;
+
     // timing
     bool timing = false;
     int bulk_kind = 0;  // D3Q19 bulk kernel variant (lbffs_set_bulk_kernel)
@@ -82,6 +89,13 @@ inline cudaError_t ctx_alloc(lbffs_ctx* c, T** p, size_t n)
     return ctx_alloc_bytes(c, reinterpret_cast<void**>(p), n * sizeof(T) + 16);
 }
 void ctx_free(lbffs_ctx* c, void* p);
+// join the asynchronous file writer, if one runs; its error, if any, becomes the context's
+int ctx_io_wait(lbffs_ctx* c);
+// join the writer and free the output state
+void ctx_output_release(lbffs_ctx* c);
+// device array of an output field (LBFFS_OUT_* or LBFFS_*MEAN); create: allocate a missing one
+// (zero-filled).  nullptr when absent (or on allocation failure with create).
+float* ctx_output_field(lbffs_ctx* c, int field, bool create);
 // create a context; arena / stream / stage are the server's (nullptr: the context owns its own)
 int ctx_create(const lbffs_desc* d, Arena* arena, cudaStream_t stream, float* stage, size_t stage_elems,
                lbffs_ctx** out);

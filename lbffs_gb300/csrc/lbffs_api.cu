@@ -117,6 +117,13 @@ static void* field_ptr(lbffs_ctx* c, int f)
         case LBFFS_GXIBM: return c->g[0];
         case LBFFS_GYIBM: return c->g[1];
         case LBFFS_GZIBM: return c->g[2];
+        case LBFFS_OUT_RHO:
+        case LBFFS_OUT_U:
+        case LBFFS_OUT_V:
+        case LBFFS_OUT_W:
+        case LBFFS_UMEAN:
+        case LBFFS_VMEAN:
+        case LBFFS_WMEAN: return ctx_output_field(c, f, false);
         default: return nullptr;
     }
 }
@@ -134,6 +141,7 @@ extern "C" int lbffs_destroy(lbffs_ctx* c)
     if (!c) return LBFFS_OK;
     cudaSetDevice(c->d.device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    ctx_output_release(c);
     void* ptrs[] = {c->f[0], c->f[1], c->iarr[0], c->iarr[1], c->iarr[2], c->iarr[3], c->solid, c->nei, c->flags,
                     c->bc, c->u0, c->v0, c->w0, c->omega, c->sdf, c->fw[0], c->fw[1], c->fw[2], c->g[0], c->g[1],
                     c->g[2], c->special, c->d_err, c->partial, c->markers, c->gm, c->ibm_acc,
@@ -399,6 +407,10 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
     if (bytes != field_bytes(c, field))
         return fail(c, LBFFS_E_ARG, "lbffs_upload: field " + std::to_string(field) + " expects " +
                                          std::to_string(field_bytes(c, field)) + " bytes, got " + std::to_string(bytes));
+    {
+        const int rc = ctx_io_wait(c);  // an asynchronous file write may still read the fields
+        if (rc != LBFFS_OK) return rc;
+    }
     CK(cudaSetDevice(c->d.device));
     FieldInfo fi = field_info(field);
     if (fi.kind == K_F) {
@@ -423,6 +435,10 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
         return LBFFS_OK;
     }
     if (field == LBFFS_GXIBM || field == LBFFS_GYIBM || field == LBFFS_GZIBM) CK(ensure_g(c));
+    if (field >= LBFFS_OUT_RHO && field <= LBFFS_OUT_W)
+        return fail(c, LBFFS_E_ARG, "lbffs_upload: the output fields are written by lbffs_output only");
+    if (field >= LBFFS_UMEAN && field <= LBFFS_WMEAN && !ctx_output_field(c, field, true))
+        return fail(c, LBFFS_E_CUDA, "lbffs_upload: cannot allocate the time-mean field");
     void* p = field_ptr(c, field);
     CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));

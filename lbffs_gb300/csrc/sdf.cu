@@ -167,6 +167,10 @@ extern "C" int lbffs_build_sdf(lbffs_ctx* c, const float* verts, const float* no
     if ((ntri > 0 && (!verts || !normals)) || !(dr >= 0.f) || !(dr < 1024.f) || !std::isfinite(dr_walls) ||
         dr_walls > 1e6f)
         return ctx_fail(c, LBFFS_E_ARG, "lbffs_build_sdf: bad argument");
+    {
+        const int rc = ctx_io_wait(c);  // an asynchronous file write may still read the geometry fields
+        if (rc != LBFFS_OK) return rc;
+    }
     cudaError_t e = cudaSetDevice(c->d.device);
     if (e != cudaSuccess) return ctx_fail(c, LBFFS_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;

@@ -125,6 +125,10 @@ extern "C" int lbffs_voxelize(lbffs_ctx* c, const float* verts, long long ntri, 
 {
     if (!c || (ntri > 0 && !verts) || ntri < 0 || ntri > (1LL << 30))
         return ctx_fail(c, LBFFS_E_ARG, "lbffs_voxelize: bad argument");
+    {
+        const int rc = ctx_io_wait(c);  // an asynchronous file write may still read the geometry fields
+        if (rc != LBFFS_OK) return rc;
+    }
     cudaError_t e = cudaSetDevice(c->d.device);
     if (e != cudaSuccess) return ctx_fail(c, LBFFS_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
