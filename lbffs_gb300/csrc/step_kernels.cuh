@@ -449,8 +449,14 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
     }
 }
 
+// Resident CTAs per SM the D3Q19 bulk kernel is compiled for (register budget 65536 / (128 x
+// this)); a build-time tuning value, 1 leaves the register count to the compiler.
+#ifndef LBFFS_BULK_MINB19
+#define LBFFS_BULK_MINB19 1
+#endif
+
 template <int Q, int S, int COLL, int SGS, bool LES>
-__global__ void __launch_bounds__(BULK_BX) k_bulk(const StepArgs a)
+__global__ void __launch_bounds__(BULK_BX, Q == 19 ? LBFFS_BULK_MINB19 : 1) k_bulk(const StepArgs a)
 {
     bulk_block<Q, S, COLL, SGS, LES>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
