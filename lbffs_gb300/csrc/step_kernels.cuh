@@ -773,19 +773,22 @@ __device__ __forceinline__ void halo_block(W* f, const uint8_t* __restrict__ fla
             axis = 2;
         }
     }
-    const long long cells = halo_face_cells(g, axis);
-    const long long per = (cells + HALO_BS - 1) / HALO_BS;
-    const int hi = blk >= per ? 1 : 0;
-    const long long p = (blk - hi * per) * HALO_BS + tid;
+    // every count below is < 2^31 (the padded plane size is, by construction of the context), so
+    // the face-cell decode runs in 32-bit arithmetic
+    const unsigned cells = (unsigned)halo_face_cells(g, axis);
+    const unsigned per = (cells + HALO_BS - 1) / HALO_BS;
+    const int hi = (unsigned)blk >= per ? 1 : 0;
+    const unsigned p = ((unsigned)blk - (unsigned)hi * per) * HALO_BS + (unsigned)tid;
     if (p >= cells) return;
     const int N[3] = {g.nx, g.ny, g.nz};
     // face cell: the face coordinate on axis, the other two from p in row-major order
     const int a0 = axis == 0 ? 1 : 0, a1 = axis == 2 ? 1 : 2;
     int x[3];
     x[axis] = hi ? N[axis] - 1 : 0;
-    x[a0] = (int)(p % N[a0]);
-    x[a1] = (int)(p / N[a0]);
-    const long long ic = ((long long)x[2] * g.ny + x[1]) * g.nx + x[0];
+    const unsigned q0 = p / (unsigned)N[a0];
+    x[a0] = (int)(p - q0 * (unsigned)N[a0]);
+    x[a1] = (int)q0;
+    const int ic = (x[2] * g.ny + x[1]) * g.nx + x[0];
     const uint8_t fl = __ldg(flags + ic);  // both loads in flight together
     const uint16_t bw = __ldg(bc + ic);
     if (fl & FL_SOLID) return;  // nobody pulls through a solid cell's ghosts
@@ -812,9 +815,10 @@ __device__ __forceinline__ void halo_block(W* f, const uint8_t* __restrict__ fla
                 up[d] -= N[d];
             }
         }
-        v[n] = miss ? __ldg(f + (long long)halo_missing<Q>(dq, bcode) * g.pE + ip)
-                    : __ldg(f + (long long)q * g.pE + g.porg + up[2] * g.pxy + up[1] * g.px + up[0]);
-        dst[n] = (long long)q * g.pE + ip - (dq.c[0] + dq.c[1] * g.px + dq.c[2] * g.pxy);
+        const int src_q = miss ? halo_missing<Q>(dq, bcode) : q;
+        const int src_i = miss ? ip : g.porg + up[2] * g.pxy + up[1] * g.px + up[0];
+        v[n] = __ldg(f + (long long)src_q * g.pE + src_i);
+        dst[n] = (long long)q * g.pE + (ip - (dq.c[0] + dq.c[1] * g.px + dq.c[2] * g.pxy));
     }
     // an x ghost sits alone in the padding sector before / after its row: writing the whole
     // 32-byte sector avoids a read-modify-write of a partly written sector
