@@ -109,6 +109,10 @@ def make_workload(name):
         n = 128
         c = K.make_case(n, n, n, 19, K.cavity_faces(0.05), nu=0.032)
         return c, dict(collision="rr", sgs="smag", wall="bb", les=0.0)
+    if name == "cavity128_q27":
+        n = 128
+        c = K.make_case(n, n, n, 27, K.cavity_faces(0.05), nu=0.032)
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=0.0)
     if name == "cavity256_q27":
         n = 256
         c = K.make_case(n, n, n, 27, K.cavity_faces(0.05), nu=0.032)
@@ -275,6 +279,7 @@ def describe(name, storage):
     return {"cavity256": f"lid-driven cavity D3Q19 RR {storage.upper()} 256^3, nu=0.032, lid 0.05 (synthetic)",
             "cavity128": f"lid-driven cavity D3Q19 RR {storage.upper()} 128^3 (synthetic, profiling size)",
             "cavity256_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256^3 (synthetic)",
+            "cavity128_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 128^3 (synthetic, profiling size)",
             "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)",
             "step768_q27": f"backward-facing step D3Q27 RR IBB LES {storage.upper()} 768x192x192, step 64, Re 5500, "
                            "sponge 64 cells (synthetic)",
