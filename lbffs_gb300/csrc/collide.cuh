@@ -21,26 +21,11 @@ namespace lbffs {
 // c_a^{n} for n in 0..2 with c in {-1,0,1}, evaluated at compile time after unrolling
 __device__ __forceinline__ float ipow(float x, int n) { return n == 0 ? 1.f : n == 1 ? x : x * x; }
 
-template <int Q>
-__device__ __forceinline__ void rr_second_order(const float (&ft)[Q], float rho, const float (&U)[3], float we,
-                                                float omega_b, float (&N2)[3][3], float (&R2)[3][3])
+// N2 (second-order non-equilibrium moments / rho) and R2 (their relaxed values plus u u) of the
+// recursive regularised collision from M2[a][b] = sum_q (c_a c_b - delta_ab / 3) f_q (upper triangle)
+__device__ __forceinline__ void rr_second_from(float (&M2)[3][3], float rho, const float (&U)[3], float we,
+                                               float omega_b, float (&N2)[3][3], float (&R2)[3][3])
 {
-    float M2[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b = 0; b < 3; b++) M2[a][b] = 0.f;
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-#pragma unroll
-            for (int b = a; b < 3; b++) {
-                const int cc = lat_c(Q, q, a) * lat_c(Q, q, b);
-                if (a == b) M2[a][b] += ((float)cc - 1.f / 3.f) * ft[q];
-                else if (cc != 0) M2[a][b] += (float)cc * ft[q];
-            }
-    }
     const float ir = 1.f / rho;
 #pragma unroll
     for (int a = 0; a < 3; a++)
@@ -63,6 +48,29 @@ __device__ __forceinline__ void rr_second_order(const float (&ft)[Q], float rho,
             R2[b][a] = R2[a][b];
         }
     }
+}
+
+template <int Q>
+__device__ __forceinline__ void rr_second_order(const float (&ft)[Q], float rho, const float (&U)[3], float we,
+                                                float omega_b, float (&N2)[3][3], float (&R2)[3][3])
+{
+    float M2[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) M2[a][b] = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = a; b < 3; b++) {
+                const int cc = lat_c(Q, q, a) * lat_c(Q, q, b);
+                if (a == b) M2[a][b] += ((float)cc - 1.f / 3.f) * ft[q];
+                else if (cc != 0) M2[a][b] += (float)cc * ft[q];
+            }
+    }
+    rr_second_from(M2, rho, U, we, omega_b, N2, R2);
 }
 
 // D3Q19 recursive regularised collision; U is the velocity with the half-force shift removed.
@@ -297,11 +305,93 @@ __device__ __forceinline__ void moments_to_pop27(float (&M)[3][3][3], float u, f
 }
 
 // D3Q27 recursive regularised collision on the tensor Hermite basis; U without the half-force shift.
+__device__ __forceinline__ void rr27_closure(float (&f)[27], float rho, const float (&U)[3], float we, float dpdx,
+                                             const float (&N2)[3][3], const float (&R2)[3][3]);
+
 __device__ __forceinline__ void collide_rr27(float (&f)[27], float rho, const float (&U)[3], float we, float omega_b,
                                              float dpdx)
 {
     float N2[3][3], R2[3][3];
     rr_second_order<27>(f, rho, U, we, omega_b, N2, R2);
+    rr27_closure(f, rho, U, we, dpdx, N2, R2);
+}
+
+// D3Q27 moments from the 13 opposite pairs (q, q + 1 for odd q): rho, j = sum c f and
+// S[a][b] = sum c_a c_b f (all components)
+struct Mom27 {
+    float rho;
+    float j[3];
+    float s[3][3];
+};
+
+__device__ __forceinline__ Mom27 moments27(const float (&f)[27])
+{
+    float a[14], d[14];
+#pragma unroll
+    for (int p = 1; p < 14; p++) {
+        a[p] = f[2 * p - 1] + f[2 * p];
+        d[p] = f[2 * p - 1] - f[2 * p];
+    }
+    Mom27 m;
+    float r = f[0];
+#pragma unroll
+    for (int p = 1; p < 14; p++) r += a[p];
+    m.rho = r;
+#pragma unroll
+    for (int x = 0; x < 3; x++) {
+        float jx = 0.f;
+#pragma unroll
+        for (int p = 1; p < 14; p++) {
+            const int c = lat_c(27, 2 * p - 1, x);
+            if (c > 0) jx += d[p];
+            else if (c < 0) jx -= d[p];
+        }
+        m.j[x] = jx;
+#pragma unroll
+        for (int y = x; y < 3; y++) {
+            float sxy = 0.f;
+#pragma unroll
+            for (int p = 1; p < 14; p++) {
+                const int cc = lat_c(27, 2 * p - 1, x) * lat_c(27, 2 * p - 1, y);
+                if (cc > 0) sxy += a[p];
+                else if (cc < 0) sxy -= a[p];
+            }
+            m.s[x][y] = m.s[y][x] = sxy;
+        }
+    }
+    return m;
+}
+
+// Pi_neq : Pi_neq of smagorinskyTauSGS from the raw second moments: sum_q c_a c_b feq_q =
+// rho delta_ab / 3 + u_a u_b for the reference's second-order equilibrium (fourth-order isotropy
+// of the velocity set)
+__device__ __forceinline__ float smag_pp_raw(const float (&S)[3][3], float rho, float u, float v, float w)
+{
+    const float r3 = rho * (1.f / 3.f);
+    const float pxx = S[0][0] - r3 - u * u, pyy = S[1][1] - r3 - v * v, pzz = S[2][2] - r3 - w * w;
+    const float pxy = S[0][1] - u * v, pxz = S[0][2] - u * w, pyz = S[1][2] - v * w;
+    return pxx * pxx + pyy * pyy + pzz * pzz + 2.f * (pxy * pxy + pxz * pxz + pyz * pyz);
+}
+
+// collide_rr27 with the second moments already summed (moments27)
+__device__ __forceinline__ void collide_rr27m(float (&f)[27], const Mom27& m, const float (&U)[3], float we,
+                                              float omega_b, float dpdx)
+{
+    float M2[3][3];
+    const float r3 = m.rho * (1.f / 3.f);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) M2[a][b] = (a == b) ? m.s[a][a] - r3 : m.s[a][b];
+    float N2[3][3], R2[3][3];
+    rr_second_from(M2, m.rho, U, we, omega_b, N2, R2);
+    rr27_closure(f, m.rho, U, we, dpdx, N2, R2);
+}
+
+// everything of the D3Q27 recursive regularised collision after the second-order moments
+__device__ __forceinline__ void rr27_closure(float (&f)[27], float rho, const float (&U)[3], float we, float dpdx,
+                                             const float (&N2)[3][3], const float (&R2)[3][3])
+{
     const float third = 1.f / 3.f, k1 = 1.f - we;
     float H[3][3][3];
 #pragma unroll

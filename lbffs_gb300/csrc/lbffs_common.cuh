@@ -47,6 +47,16 @@ constexpr uint8_t FL_FACE = 64;    // on the domain border (face codes apply)
 // bulk kernel tiling: BULK_BX threads per block, BULK_V cells per thread (32 apart)
 constexpr int BULK_BX = 128;
 constexpr int BULK_V = 2;
+// cells per thread of the D3Q27 bulk kernel (a build-time tuning value: two cells in flight per
+// thread against the register budget of 2 x 27 populations)
+#ifndef LBFFS_BULK_V27
+#define LBFFS_BULK_V27 2
+#endif
+template <int Q>
+__host__ __device__ constexpr int bulk_v()
+{
+    return Q == 19 ? BULK_V : LBFFS_BULK_V27;
+}
 
 constexpr float FP16S_SCALE = 32768.0f;  // (f - w) * 2^15 keeps |f - w| < 2 in range, 1.9e-9 above subnormals
 constexpr float FP16S_INV = 1.0f / 32768.0f;

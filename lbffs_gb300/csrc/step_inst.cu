@@ -22,7 +22,8 @@ cudaError_t LBFFS_NAME(LBFFS_Q, LBFFS_S, LBFFS_C, LBFFS_PART)(const StepArgs& a,
     const dim3 grid((unsigned)((a.n_special + SPECIAL_BS - 1) / SPECIAL_BS));
     k_special<LBFFS_Q, LBFFS_S, LBFFS_C><<<grid, SPECIAL_BS, 0, st>>>(a);
 #else
-    const dim3 grid((a.nx + BULK_BX * BULK_V - 1) / (BULK_BX * BULK_V), a.ny, a.nz);
+    constexpr int V = bulk_v<LBFFS_Q>();
+    const dim3 grid((a.nx + BULK_BX * V - 1) / (BULK_BX * V), a.ny, a.nz);
 #if LBFFS_PART == 0
     k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_SMAG, false><<<grid, BULK_BX, 0, st>>>(a);
 #elif LBFFS_PART == 1

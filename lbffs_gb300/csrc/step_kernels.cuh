@@ -236,25 +236,47 @@ __device__ __forceinline__ void bulk_collide(const StepArgs& a, float (&ft)[Q], 
         }
         const float U[3] = {u - 0.5f * a.dpdx * ir, v, w};
         collide_rr19m<HS>(ft, m, U, we, ir, a.omega_b, a.dpdx);
-    } else {
-        macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
-        if constexpr (SGS == SGS_WALE) {
-            const float own[3] = {u, v, w};
-            tsgs = wale_general(a, i, j, k, ic, own);
-        } else if constexpr (LES) {
-            tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
+    } else if constexpr (SGS != SGS_WALE) {
+        // D3Q27: one pass over the 13 opposite pairs gives rho, j and the second moments that both
+        // the Smagorinsky stress and the recursive regularised collision need
+        const Mom27 m = moments27(ft);
+        rho = m.rho;
+        const float ir = 1.f / rho;
+        u = m.j[0] * ir + 0.5f * a.dpdx * ir;  // updateRhoUVW (kernel.cl:3509-3523)
+        v = m.j[1] * ir;
+        w = m.j[2] * ir;
+        if constexpr (LES) {
+            tsgs = smag_tau(smag_pp_raw(m.s, rho, u, v, w), rho, omega, a.les, a.cs);
             if (fl & FL_SDF) tsgs = damping(tsgs, __ldg(a.sdf + ic), a.cs);
         }
         if (a.err && !(rho == rho)) atomicOr(a.err, 1);
         const float tau = sponge_tau(a, 1.f / omega, tsgs, i, j, k);
         const float we = 1.f / (tau + tsgs);
-        if (a.store_all || (fl & FL_STORE) || SGS == SGS_WALE || in_box(a, i, j, k)) {
+        if (a.store_all || (fl & FL_STORE) || in_box(a, i, j, k)) {
             a.rho_n[ic] = rho;
             a.u_n[ic] = u;
             a.v_n[ic] = v;
             a.w_n[ic] = w;
             a.tau_n[ic] = tsgs;
         }
+        if constexpr (COLL == COLL_CUMULANT) {
+            collide_cumulant(ft, rho, u, v, w, we, a.omega_b, a.clim);
+        } else {
+            const float U[3] = {u - 0.5f * a.dpdx * ir, v, w};
+            collide_rr27m(ft, m, U, we, a.omega_b, a.dpdx);
+        }
+    } else {
+        macroscopics<Q>(ft, a.dpdx, rho, u, v, w);
+        const float own[3] = {u, v, w};
+        tsgs = wale_general(a, i, j, k, ic, own);
+        if (a.err && !(rho == rho)) atomicOr(a.err, 1);
+        const float tau = sponge_tau(a, 1.f / omega, tsgs, i, j, k);
+        const float we = 1.f / (tau + tsgs);
+        a.rho_n[ic] = rho;
+        a.u_n[ic] = u;
+        a.v_n[ic] = v;
+        a.w_n[ic] = w;
+        a.tau_n[ic] = tsgs;
         collide<Q, COLL>(ft, rho, u, v, w, we, a);
     }
 }
@@ -352,36 +374,37 @@ __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)
 // instruction of a warp covers 32 consecutive cells.  Every population is pulled from the same
 // offset for every cell: cells on the domain border read the ghost layer, which k_halo filled
 // with the reference's face streaming at the start of the step.
-// One CTA tile: BULK_BX * BULK_V cells of row (j, k) starting at x-block xb.
+// One CTA tile: BULK_BX * bulk_v<Q>() cells of row (j, k) starting at x-block xb.
 template <int Q, int S, int COLL, int SGS, bool LES>
 __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int k)
 {
     using T = typename Codec<S>::T;
     constexpr bool HELD = (Q == 19);
+    constexpr int V = bulk_v<Q>();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i0 = (xb * (BULK_BX / 32) + warp) * (32 * BULK_V) + lane;
+    const int i0 = (xb * (BULK_BX / 32) + warp) * (32 * V) + lane;
     const int row = (k * a.ny + j) * a.nx;
     const int prow = pidx(a, 0, j, k);
-    uint8_t fl[BULK_V];
-    bool act[BULK_V];
+    uint8_t fl[V];
+    bool act[V];
     bool any = false;
 #pragma unroll
-    for (int v = 0; v < BULK_V; v++) {
+    for (int v = 0; v < V; v++) {
         const int i = i0 + 32 * v;
         fl[v] = (i < a.nx) ? __ldg(a.flags + row + i) : FL_SOLID;
         act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
         any |= act[v];
     }
     if (!any) return;
-    if constexpr (Q == 19 && SGS != SGS_WALE && BULK_V == 2) {
+    if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) {
         const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
         bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
         return;
     }
-    float ft[BULK_V][Q];
+    float ft[V][Q];
 #pragma unroll
-    for (int v = 0; v < BULK_V; v++) {
+    for (int v = 0; v < V; v++) {
         if (!act[v]) continue;
         const int ip = prow + i0 + 32 * v;
 #pragma unroll
@@ -391,7 +414,7 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         }
     }
 #pragma unroll
-    for (int v = 0; v < BULK_V; v++) {
+    for (int v = 0; v < V; v++) {
         if (!act[v]) continue;
         const int i = i0 + 32 * v;
         bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], i, j, k, row + i, prow + i);
