@@ -24,12 +24,14 @@ __device__ __forceinline__ float lane0(F2 a)
 {
     float x, y;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.u));
+    (void)y;
     return x;
 }
 __device__ __forceinline__ float lane1(F2 a)
 {
     float x, y;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.u));
+    (void)x;
     return y;
 }
 __device__ __forceinline__ float lane(F2 a, int v) { return v == 0 ? lane0(a) : lane1(a); }

@@ -779,11 +779,64 @@ __host__ __device__ inline long long halo_blocks(const PadGeom& g, int /*Q*/, in
     return 2LL * ((halo_face_cells(g, axis) + HALO_BS - 1) / HALO_BS);
 }
 
+// The ghosts one face cell x (on face HI of axis AX) fills: the directions that cross that face
+// inward, known at compile time, so every lattice constant of the loop folds.
+template <int Q, typename W, int AX, int HI>
+__device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)[3], uint16_t bw)
+{
+    constexpr int NQ = side_count<Q>();
+    constexpr HaloTable<Q> T{};
+    const int bcode[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
+    const bool face = (bw >> 9) & 1;
+    const int N[3] = {g.nx, g.ny, g.nz};
+    const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
+    W v[NQ];
+#pragma unroll
+    for (int n = 0; n < NQ; n++) {
+        const int q = T.side[AX][HI][n];
+        const HaloDir dq = T.d[q];
+        int up[3];
+        bool miss = false;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            up[d] = x[d] - dq.c[d];
+            if (up[d] < 0) {
+                miss |= face && is_wall_code(bcode[d]);
+                up[d] += N[d];
+            } else if (up[d] >= N[d]) {
+                miss |= face && is_wall_code(bcode[d]);
+                up[d] -= N[d];
+            }
+        }
+        const int src_q = miss ? halo_missing<Q>(dq, bcode) : q;
+        const int src_i = miss ? ip : g.porg + up[2] * g.pxy + up[1] * g.px + up[0];
+        v[n] = __ldg(f + (long long)src_q * g.pE + src_i);
+    }
+    // an x ghost sits alone in the padding sector before / after its row: writing the whole
+    // 32-byte sector avoids a read-modify-write of a partly written sector
+    constexpr int A = 32 / (int)sizeof(W);
+    const bool whole = AX == 0 && (!HI || (g.nx % A) == 0);
+#pragma unroll
+    for (int n = 0; n < NQ; n++) {
+        const int q = T.side[AX][HI][n];
+        const long long dst =
+            (long long)q * g.pE + (ip - (T.d[q].c[0] + T.d[q].c[1] * g.px + T.d[q].c[2] * g.pxy));
+        if (whole) {
+            W* sec = f + (HI ? dst : dst - (A - 1));
+            const uint32_t w32 = sizeof(W) == 4 ? (uint32_t)v[n] : ((uint32_t)v[n] | ((uint32_t)v[n] << 16));
+            const uint4 quad = make_uint4(w32, w32, w32, w32);
+            reinterpret_cast<uint4*>(sec)[0] = quad;
+            reinterpret_cast<uint4*>(sec)[1] = quad;
+        } else {
+            f[dst] = v[n];
+        }
+    }
+}
+
 template <int Q, typename W>
 __device__ __forceinline__ void halo_block(W* f, const uint8_t* __restrict__ flags, const uint16_t* __restrict__ bc,
                                            const PadGeom& g, long long b, int tid)
 {
-    constexpr int NQ = side_count<Q>();
     int axis = 0;
     long long blk = b;
     long long nb = halo_blocks(g, Q, 0);
@@ -815,49 +868,14 @@ __device__ __forceinline__ void halo_block(W* f, const uint8_t* __restrict__ fla
     const uint8_t fl = __ldg(flags + ic);  // both loads in flight together
     const uint16_t bw = __ldg(bc + ic);
     if (fl & FL_SOLID) return;  // nobody pulls through a solid cell's ghosts
-    const int bcode[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
-    const bool face = (bw >> 9) & 1;
-    const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
-    const HaloTable<Q>& tab = halo_table<Q>();
-    W v[NQ];
-    long long dst[NQ];
-#pragma unroll
-    for (int n = 0; n < NQ; n++) {
-        const int q = tab.side[axis][hi][n];
-        const HaloDir dq = tab.d[q];
-        int up[3];
-        bool miss = false;
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            up[d] = x[d] - dq.c[d];
-            if (up[d] < 0) {
-                miss |= face && is_wall_code(bcode[d]);
-                up[d] += N[d];
-            } else if (up[d] >= N[d]) {
-                miss |= face && is_wall_code(bcode[d]);
-                up[d] -= N[d];
-            }
-        }
-        const int src_q = miss ? halo_missing<Q>(dq, bcode) : q;
-        const int src_i = miss ? ip : g.porg + up[2] * g.pxy + up[1] * g.px + up[0];
-        v[n] = __ldg(f + (long long)src_q * g.pE + src_i);
-        dst[n] = (long long)q * g.pE + (ip - (dq.c[0] + dq.c[1] * g.px + dq.c[2] * g.pxy));
-    }
-    // an x ghost sits alone in the padding sector before / after its row: writing the whole
-    // 32-byte sector avoids a read-modify-write of a partly written sector
-    constexpr int A = 32 / (int)sizeof(W);
-    const bool whole = axis == 0 && (!hi || (g.nx % A) == 0);
-#pragma unroll
-    for (int n = 0; n < NQ; n++) {
-        if (whole) {
-            W* sec = f + (hi ? dst[n] : dst[n] - (A - 1));
-            const uint32_t w32 = sizeof(W) == 4 ? (uint32_t)v[n] : ((uint32_t)v[n] | ((uint32_t)v[n] << 16));
-            const uint4 quad = make_uint4(w32, w32, w32, w32);
-            reinterpret_cast<uint4*>(sec)[0] = quad;
-            reinterpret_cast<uint4*>(sec)[1] = quad;
-        } else {
-            f[dst[n]] = v[n];
-        }
+    // axis and side are uniform over the block: one specialised path each
+    switch (axis * 2 + hi) {
+        case 0: halo_cell<Q, W, 0, 0>(f, g, x, bw); break;
+        case 1: halo_cell<Q, W, 0, 1>(f, g, x, bw); break;
+        case 2: halo_cell<Q, W, 1, 0>(f, g, x, bw); break;
+        case 3: halo_cell<Q, W, 1, 1>(f, g, x, bw); break;
+        case 4: halo_cell<Q, W, 2, 0>(f, g, x, bw); break;
+        default: halo_cell<Q, W, 2, 1>(f, g, x, bw); break;
     }
 }
 
