@@ -20,20 +20,8 @@ __device__ __forceinline__ F2 pk(float x, float y)
     return r;
 }
 __device__ __forceinline__ F2 splat(float x) { return pk(x, x); }
-__device__ __forceinline__ float lane0(F2 a)
-{
-    float x, y;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.u));
-    (void)y;
-    return x;
-}
-__device__ __forceinline__ float lane1(F2 a)
-{
-    float x, y;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.u));
-    (void)x;
-    return y;
-}
+__device__ __forceinline__ float lane0(F2 a) { return __uint_as_float((unsigned)(a.u & 0xffffffffull)); }
+__device__ __forceinline__ float lane1(F2 a) { return __uint_as_float((unsigned)(a.u >> 32)); }
 __device__ __forceinline__ float lane(F2 a, int v) { return v == 0 ? lane0(a) : lane1(a); }
 
 __device__ __forceinline__ F2 operator+(F2 a, F2 b)

@@ -400,24 +400,24 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
         bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
-        return;
-    }
-    float ft[V][Q];
+    } else {
+        float ft[V][Q];
 #pragma unroll
-    for (int v = 0; v < V; v++) {
-        if (!act[v]) continue;
-        const int ip = prow + i0 + 32 * v;
+        for (int v = 0; v < V; v++) {
+            if (!act[v]) continue;
+            const int ip = prow + i0 + 32 * v;
 #pragma unroll
-        for (int q = 0; q < Q; q++) {
-            const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
-            ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+            for (int q = 0; q < Q; q++) {
+                const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
+                ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+            }
         }
-    }
 #pragma unroll
-    for (int v = 0; v < V; v++) {
-        if (!act[v]) continue;
-        const int i = i0 + 32 * v;
-        bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], i, j, k, row + i, prow + i);
+        for (int v = 0; v < V; v++) {
+            if (!act[v]) continue;
+            const int i = i0 + 32 * v;
+            bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], i, j, k, row + i, prow + i);
+        }
     }
 }
 
@@ -451,35 +451,37 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
         const int ic[2] = {(ck[0] * a.ny + cj[0]) * a.nx + ci[0], (ck[1] * a.ny + cj[1]) * a.nx + ci[1]};
         const int ip[2] = {pidx(a, ci[0], cj[0], ck[0]), pidx(a, ci[1], cj[1], ck[1])};
         bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
-        return;
-    }
-    float ft[BULK_V][Q];
+    } else {
+        float ft[BULK_V][Q];
 #pragma unroll
-    for (int v = 0; v < BULK_V; v++) {
-        if (!act[v]) continue;
-        const int ip = pidx(a, ci[v], cj[v], ck[v]);
+        for (int v = 0; v < BULK_V; v++) {
+            if (!act[v]) continue;
+            const int ip = pidx(a, ci[v], cj[v], ck[v]);
 #pragma unroll
-        for (int q = 0; q < Q; q++) {
-            const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
-            ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+            for (int q = 0; q < Q; q++) {
+                const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
+                ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+            }
         }
-    }
 #pragma unroll
-    for (int v = 0; v < BULK_V; v++) {
-        if (!act[v]) continue;
-        const int ic = (ck[v] * a.ny + cj[v]) * a.nx + ci[v];
-        bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], ci[v], cj[v], ck[v], ic, pidx(a, ci[v], cj[v], ck[v]));
+        for (int v = 0; v < BULK_V; v++) {
+            if (!act[v]) continue;
+            const int ic = (ck[v] * a.ny + cj[v]) * a.nx + ci[v];
+            bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], ci[v], cj[v], ck[v], ic, pidx(a, ci[v], cj[v], ck[v]));
+        }
     }
 }
 
-// Resident CTAs per SM the D3Q19 bulk kernel is compiled for (register budget 65536 / (128 x
-// this)); a build-time tuning value, 1 leaves the register count to the compiler.
-#ifndef LBFFS_BULK_MINB19
-#define LBFFS_BULK_MINB19 1
+// Resident CTAs per SM the D3Q19 bulk kernel may be compiled for (register budget 65536 / (128 x
+// this)); a build-time tuning value.  Left undefined, the register count is the compiler's choice.
+#ifdef LBFFS_BULK_MINB19
+#define LBFFS_BULK_BOUNDS(Q) __launch_bounds__(BULK_BX, (Q) == 19 ? LBFFS_BULK_MINB19 : 1)
+#else
+#define LBFFS_BULK_BOUNDS(Q) __launch_bounds__(BULK_BX)
 #endif
 
 template <int Q, int S, int COLL, int SGS, bool LES>
-__global__ void __launch_bounds__(BULK_BX, Q == 19 ? LBFFS_BULK_MINB19 : 1) k_bulk(const StepArgs a)
+__global__ void LBFFS_BULK_BOUNDS(Q) k_bulk(const StepArgs a)
 {
     bulk_block<Q, S, COLL, SGS, LES>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
