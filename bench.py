@@ -360,7 +360,11 @@ def run_e2e(res, steps, device):
     """Upload from pinned host memory, E2E_INNER steps, download: timed with CUDA events, the copies inside."""
     import torch
     lat, c, sel = res["lat"], res["case"], res["sel"]
-    host_in = torch.from_numpy(c.f).pin_memory()
+    f0 = c.f
+    if f0 is None:  # a case started from rest on the device: its host populations are the weights
+        from lbffs_gb300 import case as K
+        f0 = np.repeat(K.lattice(c.q)[1], c.elements)
+    host_in = torch.from_numpy(f0).pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
     stream = torch.cuda.ExternalStream(lat.stream(), device=device)
     import ctypes as C

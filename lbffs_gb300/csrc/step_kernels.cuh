@@ -396,6 +396,26 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         any |= act[v];
     }
     if (!any) return;
+#if defined(LBFFS_BULK_PREFETCH) && LBFFS_BULK_PREFETCH > 0
+    // L2 prefetch of the rows the CTA LBFFS_BULK_PREFETCH launches ahead will pull (one bulk
+    // prefetch per direction, issued by the first Q threads; the range is shrunk to whole 16-byte
+    // units inside the pulled elements, so it never leaves the population planes)
+    if (threadIdx.x < Q) {
+        const long long nb = (long long)gridDim.x * gridDim.y * gridDim.z;
+        const long long fb = (long long)blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z) +
+                             LBFFS_BULK_PREFETCH;
+        if (fb < nb) {
+            const int fx = (int)(fb % gridDim.x), fr = (int)(fb / gridDim.x);
+            const int fj = fr % a.ny, fk = fr / a.ny;
+            const int x0 = fx * BULK_BX * V, n = min(BULK_BX * V, a.nx - x0);
+            const uintptr_t base = reinterpret_cast<uintptr_t>(a.fin_s[threadIdx.x]);
+            const uintptr_t lo = base + (uintptr_t)pidx(a, x0, fj, fk) * sizeof(T);
+            const uintptr_t b0 = (lo + 15) & ~(uintptr_t)15, b1 = (lo + (uintptr_t)n * sizeof(T)) & ~(uintptr_t)15;
+            if (b1 > b0)
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b0), "r"((unsigned)(b1 - b0)) : "memory");
+        }
+    }
+#endif
     if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) {
         const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
