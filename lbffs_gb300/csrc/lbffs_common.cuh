@@ -47,10 +47,11 @@ constexpr uint8_t FL_FACE = 64;    // on the domain border (face codes apply)
 // bulk kernel tiling: BULK_BX threads per block, BULK_V cells per thread (32 apart)
 constexpr int BULK_BX = 128;
 constexpr int BULK_V = 2;
-// cells per thread of the D3Q27 bulk kernel (a build-time tuning value: two cells in flight per
-// thread against the register budget of 2 x 27 populations)
+// cells per thread of the D3Q27 bulk kernel (a build-time tuning value).  One: 27 populations per
+// thread leave room for twice the resident warps of two cells (80 against 116 registers), which
+// measured 11-15 % faster on the 768x192x192 LES step and 1.5 % on the 256^3 cavity.
 #ifndef LBFFS_BULK_V27
-#define LBFFS_BULK_V27 2
+#define LBFFS_BULK_V27 1
 #endif
 template <int Q>
 __host__ __device__ constexpr int bulk_v()

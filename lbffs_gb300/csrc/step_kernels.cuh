@@ -397,10 +397,12 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     }
     if (!any) return;
 #if defined(LBFFS_BULK_PREFETCH) && LBFFS_BULK_PREFETCH > 0
-    // L2 prefetch of the rows the CTA LBFFS_BULK_PREFETCH launches ahead will pull (one bulk
-    // prefetch per direction, issued by the first Q threads; the range is shrunk to whole 16-byte
-    // units inside the pulled elements, so it never leaves the population planes)
-    if (threadIdx.x < Q) {
+    // 2-byte D3Q19 storage: L2 prefetch of the rows the CTA LBFFS_BULK_PREFETCH launches ahead
+    // will pull (one bulk prefetch per direction, issued by the first Q threads; the range is
+    // shrunk to whole 16-byte units inside the pulled elements, so it never leaves the population
+    // planes).  The 2-byte kernel is latency-bound with half the bytes in flight of FP32; for the
+    // bandwidth-bound FP32 and D3Q27 kernels the extra requests measured slower.
+    if (Q == 19 && S != ST_FP32 && threadIdx.x < Q) {
         const long long nb = (long long)gridDim.x * gridDim.y * gridDim.z;
         const long long fb = (long long)blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z) +
                              LBFFS_BULK_PREFETCH;
