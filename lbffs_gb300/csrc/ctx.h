@@ -61,6 +61,10 @@ struct lbffs_ctx {
     lbffs::Arena* arena = nullptr;
     bool own_stream = true, own_stage = true;
 
+    // the boundary kernel runs beside the bulk kernel on a second stream (lbffs_step)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+
     // output step and asynchronous writes (output.cu)
     lbffs::OutputState* out = nullptr;
 

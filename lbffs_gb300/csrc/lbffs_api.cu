@@ -155,6 +155,9 @@ extern "C" int lbffs_destroy(lbffs_ctx* c)
         cudaEventDestroy(e.b);
     }
     for (auto e : c->pool) cudaEventDestroy(e);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
     if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBFFS_OK;
@@ -584,6 +587,14 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
     StepConfig cfg{c->d.storage, c->d.collision, c->d.sgs, c->d.wall,
                    c->d.sgs == LBFFS_SGS_SMAGORINSKY && p->les != 0.f};
     auto launch = (c->Q == 19) ? launch_q19 : launch_q27;
+    // the boundary kernel and the bulk kernel write disjoint cells and read only this step's source
+    // copy: the boundary kernel runs on a second stream, forked after the ghost fill and joined
+    // before anything that reads the step's results
+    if (c->n_special > 0 && !c->side) {
+        CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
+    }
     for (int s = 0; s < nsteps; s++) {
         StepArgs a;
         ctx_step_args(c, p, c->fcur, c->mcur, a);
@@ -604,21 +615,31 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
             if (e != cudaSuccess) return fail(c, LBFFS_E_CUDA, std::string("halo launch: ") + cudaGetErrorString(e));
         }
         float** mn = c->macro[1 - c->mcur];
-        for (int half = 0; half < 2; half++) {
+        const bool fork = c->n_special > 0;
+        if (fork) {
+            CK(cudaEventRecord(c->fork_ev, c->stream));
+            CK(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+        }
+        for (int half = 1; half >= 0; half--) {
             const bool bulk = half == 0;
-            if (!bulk && c->n_special == 0) continue;
+            if (!bulk && !fork) continue;
+            cudaStream_t st = bulk ? c->stream : c->side;
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (c->timing) {
                 e0 = get_event(c);
                 e1 = get_event(c);
-                cudaEventRecord(e0, c->stream);
+                cudaEventRecord(e0, st);
             }
-            cudaError_t e = launch(a, cfg, bulk, c->stream);
+            cudaError_t e = launch(a, cfg, bulk, st);
             if (c->timing) {
-                cudaEventRecord(e1, c->stream);
+                cudaEventRecord(e1, st);
                 c->pending.push_back({e0, e1, bulk ? 0 : 1});
             }
             if (e != cudaSuccess) return fail(c, LBFFS_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+        }
+        if (fork) {
+            CK(cudaEventRecord(c->join_ev, c->side));
+            CK(cudaStreamWaitEvent(c->stream, c->join_ev, 0));
         }
         if (c->n_markers > 1) {
             IbmArgs ia{};
