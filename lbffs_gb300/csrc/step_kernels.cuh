@@ -25,6 +25,13 @@ namespace lbffs {
 
 constexpr int SPECIAL_BS = 128;
 
+// CTAs ahead whose pulled rows a 2-byte D3Q19 bulk CTA prefetches into L2 (0: none); a build-time
+// tuning value.  608 (half a wave of 8-CTA-per-SM residency) measured 4 % faster on the 256^3
+// FP16S / BF16S cavity than none or 304, the same as 1216.
+#ifndef LBFFS_BULK_PREFETCH
+#define LBFFS_BULK_PREFETCH 608
+#endif
+
 template <int Q>
 __device__ __forceinline__ void macroscopics(const float (&ft)[Q], float dpdx, float& rho, float& u, float& v, float& w)
 {
@@ -396,7 +403,7 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         any |= act[v];
     }
     if (!any) return;
-#if defined(LBFFS_BULK_PREFETCH) && LBFFS_BULK_PREFETCH > 0
+#if LBFFS_BULK_PREFETCH > 0
     // 2-byte D3Q19 storage: L2 prefetch of the rows the CTA LBFFS_BULK_PREFETCH launches ahead
     // will pull (one bulk prefetch per direction, issued by the first Q threads; the range is
     // shrunk to whole 16-byte units inside the pulled elements, so it never leaves the population
