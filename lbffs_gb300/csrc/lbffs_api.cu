@@ -334,7 +334,7 @@ static int commit(lbffs_ctx* c)
 {
     const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
     const long long E = c->E;
-    // validate boundary codes on the device (WallFunction, code 7, is not built)
+    // validate boundary codes on the device
     {
         int* chk = nullptr;
         CK(ctx_alloc_bytes(c, (void**)&chk, 2 * sizeof(int)));
@@ -345,7 +345,6 @@ static int commit(lbffs_ctx* c)
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         ctx_free(c, chk);
         CK(e);
-        if (res[0] & 1) return fail(c, LBFFS_E_UNSUPPORTED, "boundary code 7 (WallFunction) is not supported");
         if (res[0] & 2) return fail(c, LBFFS_E_ARG, "invalid boundary code " + std::to_string(res[1]));
     }
     // sponge zone face-centre codes (tauSpongeZone, kernel.cl:2447-2501)

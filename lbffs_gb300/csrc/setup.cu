@@ -54,12 +54,13 @@ __global__ void k_classify1(const uint16_t* bc, const uint8_t* solid, const uint
             link |= (up >= 0 && solid[up] == 1);
         }
     }
-    // faces with an Outlet, FixedVelocity or FixedDensity code need the boundary operators of the
+    // faces with an Outlet, FixedVelocity, FixedDensity or WallFunction code need the boundary operators of the
     // general kernel; wall / periodic / symmetry faces only change where populations come from
     // and stay in the bulk kernel
     bool complex_bc = false;
 #pragma unroll
-    for (int d = 0; d < 3; d++) complex_bc |= (b[d] == BC_OUTLET || b[d] == BC_FIXVEL || b[d] == BC_FIXDEN);
+    for (int d = 0; d < 3; d++)
+        complex_bc |= (b[d] == BC_OUTLET || b[d] == BC_FIXVEL || b[d] == BC_FIXDEN || b[d] == BC_WALLFN);
     complex_bc &= (face || border);
     uint8_t fl = 0;
     if (face || border) fl |= FL_FACE;

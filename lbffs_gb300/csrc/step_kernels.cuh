@@ -163,6 +163,29 @@ __device__ __forceinline__ void collide(float (&ft)[Q], float rho, float u, floa
     }
 }
 
+// calcTauw (D3Q19 kernel.cl:1621-1655, D3Q27 1487-1522): wall shear stress from the tangential
+// speed magUp 1.5 cells from the wall by Newton iterations on Spalding's law (kappa 0.42, E 9.1).
+// As in the reference, the convergence test compares each new y+ with the first one (the
+// loop's yPlus update declares a new variable), for at most 100 iterations.
+__device__ __forceinline__ float calc_tauw(float rhow, float magUp, float nu)
+{
+    const float y = 1.5f, kappa = 0.42f, E = 9.1f;
+    float ut = sqrtf(nu * magUp);
+    const float yPlus = y * ut / nu;
+    int iter = 0;
+    float err;
+    do {
+        const float kUu = fminf(kappa * magUp / ut, 50.f);
+        const float fkUu = expf(kUu) - 1.f - kUu * (1.f + 0.5f * kUu);
+        const float func = -ut * y / nu + magUp / ut + (fkUu - kUu * kUu * kUu / 6.f) / E;
+        const float dfunc = y / nu + magUp / (ut * ut) + (kUu * fkUu / ut) / E;
+        ut = ut + func / dfunc;
+        err = fabsf(yPlus - y * ut / nu);
+    } while (err > 0.005f && ++iter < 100);
+    ut = fmaxf(ut, 0.f);
+    return rhow * ut * ut;
+}
+
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ bool is_wall_code(int b) { return b == 1 || b == 4 || b == 5 || b == 6 || b == 7; }
 
@@ -552,7 +575,11 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     for (int q = 0; q < Q; q++) ft[q] = Codec<S>::load(static_cast<const T*>(a.fin_s[q]) + ip, lat_w(Q, q));
 
     const float uo[3] = {a.u_p[ic], a.v_p[ic], a.w_p[ic]};
+    const float omega_c = a.omega[ic];
     if (face) {
+        float fts[Q];  // the streamed values (the bounce-back momentum of the wall function uses them)
+#pragma unroll
+        for (int q = 0; q < Q; q++) fts[q] = ft[q];
         // cornerFlag (kernel.cl:1346-1397)
         const bool on0 = x[0] == 0 || x[0] == N[0] - 1, on1 = x[1] == 0 || x[1] == N[1] - 1,
                    on2 = x[2] == 0 || x[2] == N[2] - 1;
@@ -603,6 +630,66 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
                         const float cu = (float)lat_c(Q, q, 0) * uw[0] + (float)lat_c(Q, q, 1) * uw[1] + (float)lat_c(Q, q, 2) * uw[2];
                         ft[q] = -ft[q] + 2.f * lat_w(Q, q) * (1.f + 4.5f * cu * cu - 1.5f * usq);
                     }
+                }
+            }
+        }
+        if (!corner) {
+            // wallFunctionBC (D3Q19 kernel.cl:1657-1924, D3Q27 1524-): a stationary wall whose
+            // tangential slip velocity comes from the log-law shear stress of the cell 1 inward,
+            // minus the momentum the face's bounce-back exchanged in this step's streaming (which
+            // the reference's streaming() leaves in Fw before internalWallBC resets it), applied as
+            // a moving-wall correction to the populations entering from the face.  Per axis the low
+            // face wins over the high one (if / else if).
+            const float nu = (1.f / omega_c - 0.5f) / 3.f;
+            float fwc[3] = {0.f, 0.f, 0.f};
+            if (b[0] == BC_WALLFN || b[1] == BC_WALLFN || b[2] == BC_WALLFN) {
+#pragma unroll
+                for (int q = 1; q < Q; q++) {
+                    if (upwind<Q>(q, x, N, b, face) >= 0) continue;
+#pragma unroll
+                    for (int dd = 0; dd < 3; dd++)
+                        if (lat_c(Q, q, dd)) fwc[dd] += -2.f * fts[q] * (float)lat_c(Q, q, dd);
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                if (b[d] != BC_WALLFN) continue;
+                int side;
+                if (x[d] == 0) side = -1;
+                else if (x[d] == N[d] - 1) side = 1;
+                else continue;
+                const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;  // tangential axes, in order
+                float tang = 0.f, outg = 0.f;
+#pragma unroll
+                for (int q = 0; q < Q; q++) {
+                    if (lat_c(Q, q, d) == 0) tang += ft[q];
+                    else if (lat_c(Q, q, d) == side) outg += ft[q];
+                }
+                const float rhow = tang + 2.f * outg;
+                // the probe 1 cell inward (a 1-cell axis: the cell itself; the reference's z-max face
+                // reads k + 1, outside the grid: here k - 1)
+                const long long pr = (d == 2 && N[2] == 1) ? ic : inner(d, side);
+                const float up[3] = {a.u_p[pr], a.v_p[pr], a.w_p[pr]};
+                float mag = sqrtf(up[t1] * up[t1] + up[t2] * up[t2]);
+                float tw[3] = {0.f, 0.f, 0.f};  // wall velocity (normal component stays 0)
+                if (mag != 0.f) {
+                    const float tauw = calc_tauw(rhow, mag, nu);
+                    mag = sqrtf(uo[t1] * uo[t1] + uo[t2] * uo[t2]);
+                    // the z-min face of the reference does not test the cell's own speed
+                    if (mag != 0.f || (d == 2 && side < 0)) {
+                        tw[t1] = -3.f * (tauw * (uo[t1] / mag) - fwc[t1]) / rhow;
+                        tw[t2] = -3.f * (tauw * (uo[t2] / mag) - fwc[t2]) / rhow;
+                    }
+                }
+                const int n = -side;  // inward direction along d
+#pragma unroll
+                for (int q = 1; q < Q; q++) {
+                    if (lat_c(Q, q, d) != n || lat_n2(Q, q) == 1) continue;  // axis term: rho_w * 0
+                    float s = 0.f;  // the wall's normal speed, then the tangential terms
+                    if (lat_c(Q, q, t1)) s += (float)(lat_c(Q, q, t1) * n) * tw[t1];
+                    if (lat_c(Q, q, t2)) s += (float)(lat_c(Q, q, t2) * n) * tw[t2];
+                    const float den = lat_n2(Q, q) == 2 ? (Q == 19 ? 6.f : 9.f) : 36.f;
+                    ft[q] += (float)n * (rhow * s) / den;
                 }
             }
         }

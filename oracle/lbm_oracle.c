@@ -268,6 +268,83 @@ static void fixed_density(const ctx* X, real* ft, const int b[3], long ic, const
     }
 }
 
+/* calcTauw (D3Q19 kernel.cl:1621-1655, D3Q27 kernel.cl:1487-1522): Newton iterations on
+ * Spalding's law for the friction velocity 1.5 cells from the wall.  The reference's loop updates a
+ * y+ declared inside the loop body, so its convergence test always compares with the first y+. */
+static real calc_tauw(real rhow, real magUp, real nu)
+{
+    const real y = (real)1.5, kappa = (real)0.42, Ek = (real)9.1;
+    real ut = sqrt(nu * magUp);
+    const real yPlus = y * ut / nu;
+    int iter = 0;
+    real err;
+    do {
+        real kUu = fmin(kappa * magUp / ut, (real)50);
+        real fkUu = exp(kUu) - (real)1 - kUu * ((real)1 + (real)0.5 * kUu);
+        real func = -ut * y / nu + magUp / ut + (fkUu - kUu * kUu * kUu / (real)6) / Ek;
+        real dfunc = y / nu + magUp / (ut * ut) + (kUu * fkUu / ut) / Ek;
+        ut = ut + func / dfunc;
+        err = fabs(yPlus - y * ut / nu);
+    } while (err > (real)0.005 && ++iter < 100);
+    ut = fmax(ut, (real)0);
+    return rhow * ut * ut;
+}
+
+/* wallFunctionBC (D3Q19 kernel.cl:1657-1924, D3Q27 kernel.cl:1524-): on a face with code 7 the
+ * populations entering from the wall get a moving-wall correction whose tangential velocity is
+ * -3 (tau_w e_t - Fw_t) / rho_w, tau_w from the previous-step tangential speed one cell inward and
+ * e_t the direction of the cell's own previous-step tangential velocity.  Fw is the momentum the
+ * face's bounce-back exchanged in this step's streaming (streaming(), D3Q19 kernel.cl:1281-1312,
+ * writes it before internalWallBC resets the field).  Per axis the low face takes precedence
+ * (if / else if); the z-max face probes k - 1 (the reference reads k + 1, outside the grid); the
+ * z-min face does not test the own speed for zero, as in the reference. */
+static void wall_function(const ctx* X, real* ft, const int b[3], long ic, const int x[3], real omega,
+                          const real fw[3])
+{
+    const lat* L = &X->L;
+    const or_fields* A = X->a;
+    const real nu = ((real)1 / omega - (real)0.5) / (real)3;
+    const real uo[3] = {A->uPrev[ic], A->vPrev[ic], A->wPrev[ic]};
+    for (int a = 0; a < 3; a++) {
+        if (b[a] != BC_WALLFN) continue;
+        int side;
+        if (x[a] == 0) side = -1;
+        else if (x[a] == X->N[a] - 1) side = 1;
+        else continue;
+        const int t1 = a == 0 ? 1 : 0, t2 = a == 2 ? 1 : 2;
+        real tang = 0, outg = 0;
+        for (int q = 0; q < L->Q; q++) {
+            if (L->c[q][a] == 0) tang += ft[q];
+            else if (L->c[q][a] == side) outg += ft[q];
+        }
+        const real rhow = tang + (real)2 * outg;
+        int y[3] = {x[0], x[1], x[2]};
+        if (!(a == 2 && X->N[2] == 1)) y[a] = side < 0 ? (X->N[a] > 1 ? 1 : 0) : (X->N[a] > 1 ? X->N[a] - 2 : 0);
+        const long pr = idx(X, y[0], y[1], y[2]);
+        const real up[3] = {A->uPrev[pr], A->vPrev[pr], A->wPrev[pr]};
+        real mag = sqrt(up[t1] * up[t1] + up[t2] * up[t2]);
+        real tw[3] = {0, 0, 0};
+        if (mag != (real)0) {
+            const real tauw = calc_tauw(rhow, mag, nu);
+            mag = sqrt(uo[t1] * uo[t1] + uo[t2] * uo[t2]);
+            if (mag != (real)0 || (a == 2 && side < 0)) {
+                tw[t1] = (real)-3 * (tauw * (uo[t1] / mag) - fw[t1]) / rhow;
+                tw[t2] = (real)-3 * (tauw * (uo[t2] / mag) - fw[t2]) / rhow;
+            }
+        }
+        const int n = -side;
+        for (int q = 1; q < L->Q; q++) {
+            const int nz = (L->c[q][0] != 0) + (L->c[q][1] != 0) + (L->c[q][2] != 0);
+            if (L->c[q][a] != n || nz == 1) continue;
+            real sum = 0;
+            if (L->c[q][t1]) sum += (real)(L->c[q][t1] * n) * tw[t1];
+            if (L->c[q][t2]) sum += (real)(L->c[q][t2] * n) * tw[t2];
+            const real den = nz == 2 ? (L->Q == 19 ? (real)6 : (real)9) : (real)36;
+            ft[q] += (real)n * (rhow * sum) / den;
+        }
+    }
+}
+
 /* outflowBC (Geier et al. 2015 App. F; D3Q19 kernel.cl:2005-2097, D3Q27 kernel.cl:1900-1991):
  * incoming populations blend the inner and own previous post-collision values with the own
  * previous velocity component of that axis.  Later faces overwrite earlier ones. */
@@ -515,14 +592,20 @@ static void cell_step(const ctx* X, long ic)
     ft[0] = f[ic];
     up[0] = ic;
     if (A->boundary[ic] == 1) {
+        real fws[3] = {0, 0, 0};  /* bounce-back momentum of the face (streaming(), kernel.cl:1281-1312) */
         for (int q = 1; q < L->Q; q++) {
             up[q] = upwind_face(X, q, x, b);
-            if (up[q] >= 0) ft[q] = f[(long)q * E + up[q]];
-            else ft[q] = f[(long)missing_dir(X, q, b) * E + ic];
+            if (up[q] >= 0) {
+                ft[q] = f[(long)q * E + up[q]];
+            } else {
+                ft[q] = f[(long)missing_dir(X, q, b) * E + ic];
+                for (int a = 0; a < 3; a++) fws[a] += (real)-2 * ft[q] * (real)L->c[q][a];
+            }
         }
         if (!corner_flag(X, b[2], x)) {
             fixed_velocity(X, ft, uw, b, ic, x);
             fixed_density(X, ft, b, ic, x);
+            wall_function(X, ft, b, ic, x, omega, fws);
         }
         outflow(X, ft, f, uo, b, ic, x);
     } else {
@@ -594,8 +677,6 @@ int oracle_step(const or_config* cfg, or_fields* a, const or_params* p, const or
     init_ctx(&X, cfg, p, a);
     const long E = X.E;
     const int nt = p->nthreads > 0 ? p->nthreads : omp_get_max_threads();
-    for (long ic = 0; ic < E; ic++)
-        if (a->boundary1[ic] == BC_WALLFN || a->boundary2[ic] == BC_WALLFN || a->boundary3[ic] == BC_WALLFN) return -2;
     for (int s = 0; s < nsteps; s++) {
         memcpy(a->rhoPrev, a->rho, sizeof(real) * E);
         memcpy(a->uPrev, a->u, sizeof(real) * E);

@@ -10,7 +10,7 @@ build; its velocity and the FP32-vs-FP64 distance of the reference itself
 reference checkout, so it runs in the build container; the .npz files it writes
 are committed and travel with the tests.
 
-usage: python tests/golden/make_golden.py
+usage: python tests/golden/make_golden.py [case ...]   (default: every case)
 """
 import os
 import sys
@@ -26,8 +26,8 @@ from oracle.ref import RefSolver  # noqa: E402
 from parity_cases import REFERENCE_CASES, build  # noqa: E402
 
 
-def main():
-    for name in REFERENCE_CASES:
+def main(names=None):
+    for name in names or REFERENCE_CASES:
         c, run = build(name)
         r = RefSolver(c, sgs=run["sgs"], wall=run["wall"], real="f32", nthreads=1)
         if "markers" in run:
@@ -57,4 +57,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

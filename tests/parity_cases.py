@@ -9,8 +9,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from lbffs_gb300.case import (BOUNCEBACK, CYCLIC, FIXEDDENSITY, FIXEDVELOCITY, OUTLET, SYMMETRY, FaceBC,
-                              cavity_faces, channel_faces, make_case)
+from lbffs_gb300.case import (BOUNCEBACK, CYCLIC, FIXEDDENSITY, FIXEDVELOCITY, OUTLET, SYMMETRY, WALLFUNCTION,
+                              FaceBC, cavity_faces, channel_faces, make_case)
 from lbffs_gb300.geometry import backward_step, cylinder_markers, cylinder_z
 
 
@@ -23,6 +23,12 @@ def _mixed_faces():
 def _density_faces():
     f = channel_faces(0.05, top_bottom=BOUNCEBACK, z_periodic=False)
     f["nxMax"] = FaceBC(FIXEDDENSITY, CYCLIC, CYCLIC)
+    return f
+
+
+def _wallfn_faces():
+    """Channel whose y faces are WallFunction walls (code 7), z periodic."""
+    f = channel_faces(0.05, top_bottom=WALLFUNCTION, z_periodic=True)
     return f
 
 
@@ -76,13 +82,19 @@ def build(name):
         m = cylinder_markers(24, 11.3, 9.7, 2.4, 3.2)
         return c, dict(sgs="smag", wall="bb", collision="rr", steps=30, kw={}, markers=m,
                        motion=dict(trans=(0.01, 0.0, 0.0)))
+    if name == "wallfn_q19":
+        c = make_case(32, 16, 6, 19, _wallfn_faces(), nu=0.004)
+        return c, dict(sgs="smag", wall="bb", collision="rr", steps=40, kw={})
+    if name == "wallfn_q27":
+        c = make_case(28, 14, 6, 27, _wallfn_faces(), nu=0.004)
+        return c, dict(sgs="smag", wall="ibb", collision="cumulant", steps=30, kw={})
     raise KeyError(name)
 
 
 # cases the reference itself can run (golden vectors are recorded from it)
 REFERENCE_CASES = ["cavity_q19", "cavity_q19_les", "cavity_q19_wale", "cylinder_q19_ibb_les_sponge", "cylinder_q19_bb",
                    "cylinder2d_q19_ibb", "mixed_q19", "density_q19_dpdx", "step_q19_les", "mixed_q27_cumulant",
-                   "cylinder_q27_cumulant_les", "cavity_q27_wale", "ibm_q19"]
+                   "cylinder_q27_cumulant_les", "cavity_q27_wale", "ibm_q19", "wallfn_q19", "wallfn_q27"]
 
 
 def rel_err(a, b):

@@ -206,11 +206,11 @@ def test_errors_are_status_codes(cuda_lib):
     c = K.make_case(8, 8, 8, 19, K.cavity_faces(0.05))
     lat.load_case(c)
     b1 = c.boundary1.copy()
-    b1[b1 == K.BOUNCEBACK] = K.WALLFUNCTION
+    b1[b1 == K.BOUNCEBACK] = 2  # no boundary code 2 exists (src/input.hpp:221-256)
     lat.upload("boundary1", b1)
     with pytest.raises(L.LbffsError) as e:
         lat.step(1)
-    assert e.value.code == L.E_UNSUPPORTED
+    assert e.value.code == L.E_ARG
 
 
 def test_divergence_sentinel_reports_nonfinite(cuda_lib):
