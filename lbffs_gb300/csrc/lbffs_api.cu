@@ -590,7 +590,11 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
     // copy: the boundary kernel runs on a second stream, forked after the ghost fill and joined
     // before anything that reads the step's results
     if (c->n_special > 0 && !c->side) {
-        CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+        // the higher priority lets the small boundary kernel take SMs as the bulk kernel's CTAs
+        // retire instead of waiting behind all of them
+        int lo = 0, hi = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        CK(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, hi));
         CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
     }

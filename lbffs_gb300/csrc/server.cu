@@ -9,7 +9,8 @@
 //      LES switch: the cases' kernel arguments for both parities, the prefix sums of bulk tiles
 //      and special cells) and captures steps_per_round steps into a CUDA graph;
 //   3. replays the graph once: every step is one batched ghost-layer, bulk and special launch per
-//      group plus a counter tick, so all resident cases advance together, each case's device
+//      group (the special launches on a parallel branch beside the bulk ones) plus a counter tick,
+//      so all resident cases advance together, each case's device
 //      step counter choosing its ping-pong parity and stopping it at exactly its nsteps;
 //   4. reads back the counters and retires finished cases: their final fields are downloaded and
 //      their arena blocks released, which lets the next round admit more.
@@ -88,6 +89,8 @@ struct lbffs_server {
     cudaStream_t stream = nullptr;         // batched steps (graph replay)
     cudaStream_t setup_stream = nullptr;   // admission: per-case uploads and commits
     cudaStream_t result_stream = nullptr;  // retirement: result downloads
+    cudaStream_t branch = nullptr;         // captured graph: the boundary kernels' parallel branch
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     void* arena_mem = nullptr;
     std::unique_ptr<Arena> arena;
     float* stage = nullptr;   // admission staging
@@ -334,18 +337,28 @@ cudaError_t build_batch(lbffs_server* s)
     cudaGraph_t graph = nullptr;
     if ((e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal))) return e;
     cudaError_t le = cudaSuccess;
+    bool any_special = false;
+    for (Group& g : s->groups) any_special |= g.nspecial > 0;
     for (int step = 0; step < s->d.steps_per_round && le == cudaSuccess; step++) {
         for (Group& g : s->groups)
             if (le == cudaSuccess && g.nhalo > 0)
                 le = batch_halo(g.storage, g.d_cases, g.d_halo, (int)g.members.size(), g.nhalo, s->d_done, s->stream);
+        // the boundary kernels write other cells than the bulk kernels and read the same source
+        // copy: a parallel branch of the graph, joined before the counter tick
+        if (le == cudaSuccess && any_special) {
+            le = cudaEventRecord(s->fork_ev, s->stream);
+            if (le == cudaSuccess) le = cudaStreamWaitEvent(s->branch, s->fork_ev, 0);
+            for (Group& g : s->groups)
+                if (le == cudaSuccess && g.nspecial > 0)
+                    le = batch_special(g.storage, g.d_cases, g.d_sp, (int)g.members.size(), g.nspecial, s->d_done,
+                                       s->branch);
+            if (le == cudaSuccess) le = cudaEventRecord(s->join_ev, s->branch);
+        }
         for (Group& g : s->groups)
             if (le == cudaSuccess && g.ntiles > 0)
                 le = batch_bulk(g.storage, g.les, g.d_cases, g.d_tiles, (int)g.members.size(), g.ntiles, s->d_done,
                                 s->stream);
-        for (Group& g : s->groups)
-            if (le == cudaSuccess && g.nspecial > 0)
-                le = batch_special(g.storage, g.d_cases, g.d_sp, (int)g.members.size(), g.nspecial, s->d_done,
-                                   s->stream);
+        if (le == cudaSuccess && any_special) le = cudaStreamWaitEvent(s->stream, s->join_ev, 0);
         if (le == cudaSuccess) le = batch_tick(s->d_tick_slots, s->d_tick_nsteps, s->ntick, s->d_done, s->stream);
     }
     e = cudaStreamEndCapture(s->stream, &graph);
@@ -579,6 +592,11 @@ extern "C" int lbffs_server_create(const lbffs_server_desc* desc, lbffs_server**
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->setup_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->result_stream, cudaStreamNonBlocking);
+    int prio_lo = 0, prio_hi = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->branch, cudaStreamNonBlocking, prio_hi);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&s->arena_mem, desc->hbm_budget);
@@ -637,6 +655,9 @@ extern "C" int lbffs_server_destroy(lbffs_server* s)
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->setup_stream) cudaStreamDestroy(s->setup_stream);
     if (s->result_stream) cudaStreamDestroy(s->result_stream);
+    if (s->branch) cudaStreamDestroy(s->branch);
+    if (s->fork_ev) cudaEventDestroy(s->fork_ev);
+    if (s->join_ev) cudaEventDestroy(s->join_ev);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     delete s;
