@@ -33,7 +33,7 @@ extern "C" {
 #define LBFFS_E_ARG (-1)     /* invalid argument (size, field id, enum value) */
 #define LBFFS_E_CUDA (-2)    /* a CUDA runtime call failed; see lbffs_last_error */
 #define LBFFS_E_STATE (-3)   /* call not valid in the current state */
-#define LBFFS_E_UNSUPPORTED (-4) /* feature present in the reference but not built (WallFunction code 7) */
+#define LBFFS_E_UNSUPPORTED (-4) /* a combination the called entry point does not serve */
 #define LBFFS_E_NONFINITE (-5)   /* a non-finite density was produced (divergence sentinel) */
 
 typedef struct lbffs_ctx lbffs_ctx;
