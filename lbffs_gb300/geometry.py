@@ -33,6 +33,19 @@ def cylinder_z(nx, ny, nz, cx, cy, radius, sdf_band=10.0):
     return solid, sdf
 
 
+def ellipsoid(nx, ny, nz, center, radii, sdf_band=10.0):
+    """Ellipsoid body: solid mask and an approximate signed distance (fluid > 0) within sdf_band,
+    (|x / r| - 1) scaled by the smallest radius (exact on the sphere, first order elsewhere)."""
+    i, j, k = _grid(nx, ny, nz)
+    rr = np.sqrt(((i - center[0]) / radii[0]) ** 2 + ((j - center[1]) / radii[1]) ** 2 +
+                 ((k - center[2]) / radii[2]) ** 2)
+    d = (rr - 1.0) * min(radii)
+    solid = (d < 0).astype(np.uint8).ravel()
+    sdf = d.astype(np.float32).ravel()
+    sdf[np.abs(sdf) > sdf_band] = SDF_NONE
+    return solid, sdf
+
+
 def backward_step(nx, ny, nz, x_end, height, sdf_band=3.0):
     """Solid block j < height for i < x_end (backward-facing step); distance to the block's faces."""
     i, j, _ = _grid(nx, ny, nz)

@@ -11,7 +11,7 @@ import numpy as np
 
 from lbffs_gb300.case import (BOUNCEBACK, CYCLIC, FIXEDDENSITY, FIXEDVELOCITY, OUTLET, SYMMETRY, WALLFUNCTION,
                               FaceBC, cavity_faces, channel_faces, make_case)
-from lbffs_gb300.geometry import backward_step, cylinder_markers, cylinder_z
+from lbffs_gb300.geometry import backward_step, cylinder_markers, cylinder_z, ellipsoid
 
 
 def _mixed_faces():
@@ -82,6 +82,14 @@ def build(name):
         m = cylinder_markers(24, 11.3, 9.7, 2.4, 3.2)
         return c, dict(sgs="smag", wall="bb", collision="rr", steps=30, kw={}, markers=m,
                        motion=dict(trans=(0.01, 0.0, 0.0)))
+    if name == "bluff_q27_les_ibm":
+        # the bluff-body configuration at reduced size: D3Q27, an ellipsoid body with interpolated
+        # bounce-back, LES, and an IBM cylinder upstream (two marker rings, translating)
+        solid, sdf = ellipsoid(48, 20, 20, (26.3, 9.8, 10.2), (9.0, 4.2, 4.4))
+        c = make_case(48, 20, 20, 27, channel_faces(0.05), nu=0.002, solid=solid, sdf=sdf)
+        m = np.concatenate([cylinder_markers(16, 8.2, 9.6, 9.5 + z, 2.5) for z in range(2)])
+        return c, dict(sgs="smag", wall="ibb", collision="cumulant", steps=30, kw=dict(LES=1.0), markers=m,
+                       motion=dict(trans=(0.0, 0.004, 0.0)))
     if name == "wallfn_q19":
         c = make_case(32, 16, 6, 19, _wallfn_faces(), nu=0.004)
         return c, dict(sgs="smag", wall="bb", collision="rr", steps=40, kw={})
@@ -94,7 +102,8 @@ def build(name):
 # cases the reference itself can run (golden vectors are recorded from it)
 REFERENCE_CASES = ["cavity_q19", "cavity_q19_les", "cavity_q19_wale", "cylinder_q19_ibb_les_sponge", "cylinder_q19_bb",
                    "cylinder2d_q19_ibb", "mixed_q19", "density_q19_dpdx", "step_q19_les", "mixed_q27_cumulant",
-                   "cylinder_q27_cumulant_les", "cavity_q27_wale", "ibm_q19", "wallfn_q19", "wallfn_q27"]
+                   "cylinder_q27_cumulant_les", "cavity_q27_wale", "ibm_q19", "wallfn_q19", "wallfn_q27",
+                   "bluff_q27_les_ibm"]
 
 
 def rel_err(a, b):

@@ -126,6 +126,19 @@ def test_fp16s_velocity_error_vs_fp64_oracle(cuda_lib, oracle_built):
     assert out["bf16s"] < 5e-2, out
 
 
+@pytest.mark.parametrize("name", ["bluff_q27_les_ibm", "step_q19_les", "wallfn_q19"])
+def test_fp16s_boundary_cases_vs_fp64_oracle(cuda_lib, oracle_built, name):
+    """FP16S storage on the reduced bluff body (D3Q27, IBB, LES, IBM), the LES backward-facing step
+    and the wall-function channel: relative L2 velocity error against the FP64 oracle <= 1e-3."""
+    c, run = build(name)
+    o = run_oracle(name, real="f64")
+    fluid = c.solid == 0
+    ref = np.stack([o.field(k)[fluid] for k in ("u", "v", "w")])
+    _, _, lat = run_gpu(name, storage="fp16s")
+    vel = np.stack([lat.download(k)[fluid] for k in ("u", "v", "w")])
+    assert rel_l2(vel, ref) < 1e-3, rel_l2(vel, ref)
+
+
 def test_storage_modes_agree_with_each_other(cuda_lib):
     res = {}
     for st in ("fp32", "fp16s"):
