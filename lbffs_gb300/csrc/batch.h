@@ -18,8 +18,12 @@ struct BatchCase {
 
 // x segments one bulk tile covers (BULK_V per warp of a BULK_BX-thread CTA; bulk_segments)
 constexpr int BATCH_SEG_PER_TILE = (BULK_BX / 32) * BULK_V;
-// bulk tiles one CTA of the batched kernel runs (one case's argument copy serves them all)
-constexpr int BATCH_TILES_PER_CTA = 8;
+// bulk tiles one CTA of the batched kernel runs (one case's argument copy serves them all); a
+// build-time tuning value
+#ifndef LBFFS_BATCH_TILES
+#define LBFFS_BATCH_TILES 8
+#endif
+constexpr int BATCH_TILES_PER_CTA = LBFFS_BATCH_TILES;
 
 // Bulk step of every case in cases[0..ncases), in the segment mapping of bulk_segments (narrow
 // rows keep the lanes busy): CTA b runs run b - tile_start[c] of the case c

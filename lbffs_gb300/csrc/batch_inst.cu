@@ -28,8 +28,19 @@ __device__ __forceinline__ int find_case(const T* __restrict__ start, int n, T k
     return lo;
 }
 
+// resident CTAs per SM the batched bulk kernel is compiled for (0: the compiler's choice); a
+// build-time tuning value
+#ifndef LBFFS_BATCH_MINB
+#define LBFFS_BATCH_MINB 8
+#endif
+#if LBFFS_BATCH_MINB > 0
+#define LBFFS_BATCH_BOUNDS __launch_bounds__(BULK_BX, LBFFS_BATCH_MINB)
+#else
+#define LBFFS_BATCH_BOUNDS __launch_bounds__(BULK_BX)
+#endif
+
 template <bool LES>
-__global__ void __launch_bounds__(BULK_BX, 8) k_bulk_batch(const BatchCase* __restrict__ cases,
+__global__ void LBFFS_BATCH_BOUNDS k_bulk_batch(const BatchCase* __restrict__ cases,
                                                         const int* __restrict__ tile_start, int ncases,
                                                         const long long* __restrict__ done)
 {
