@@ -19,9 +19,10 @@ struct BatchCase {
 // x segments one bulk tile covers (BULK_V per warp of a BULK_BX-thread CTA; bulk_segments)
 constexpr int BATCH_SEG_PER_TILE = (BULK_BX / 32) * BULK_V;
 // bulk tiles one CTA of the batched kernel runs (one case's argument copy serves them all); a
-// build-time tuning value
+// build-time tuning value.  On the 48-request served sample 4 measured best (GPU busy time
+// 1.818 s; 1: 1.859 s, 2: 1.815 s, 8: 1.845 s).
 #ifndef LBFFS_BATCH_TILES
-#define LBFFS_BATCH_TILES 8
+#define LBFFS_BATCH_TILES 4
 #endif
 constexpr int BATCH_TILES_PER_CTA = LBFFS_BATCH_TILES;
 
