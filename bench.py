@@ -109,6 +109,9 @@ def make_workload(name):
         n = 128
         c = K.make_case(n, n, n, 19, K.cavity_faces(0.05), nu=0.032)
         return c, dict(collision="rr", sgs="smag", wall="bb", les=0.0)
+    if name == "cavity256x64":
+        c = K.make_case(256, 256, 64, 19, K.cavity_faces(0.05), nu=0.032)
+        return c, dict(collision="rr", sgs="smag", wall="bb", les=0.0)
     if name == "cavity128_q27":
         n = 128
         c = K.make_case(n, n, n, 27, K.cavity_faces(0.05), nu=0.032)
@@ -278,6 +281,8 @@ def run_serving(n_req, step_scale, device, budget_gb=150.0):
 def describe(name, storage):
     return {"cavity256": f"lid-driven cavity D3Q19 RR {storage.upper()} 256^3, nu=0.032, lid 0.05 (synthetic)",
             "cavity128": f"lid-driven cavity D3Q19 RR {storage.upper()} 128^3 (synthetic, profiling size)",
+            "cavity256x64": f"lid-driven cavity D3Q19 RR {storage.upper()} 256x256x64 (synthetic, profiling size: "
+                            "the 256-cell rows of the 256^3 case, populations larger than L2)",
             "cavity256_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256^3 (synthetic)",
             "cavity128_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 128^3 (synthetic, profiling size)",
             "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)",

@@ -1,6 +1,6 @@
-// Launchers of the row-staged D3Q19 bulk kernel (bulk_tma.cuh), compiled once per storage
-// format (LBFFS_S).  The grid is persistent: as many CTAs as fit on the device at once, each
-// walking the row tiles with a stride of the grid size.
+// Launchers of the warp-specialised D3Q19 bulk kernel (bulk_tma.cuh), compiled once per
+// storage format (LBFFS_S).  The grid is persistent: as many CTAs as fit on the device at once,
+// each walking the row tiles with a stride of the grid size.
 #include "bulk_tma.cuh"
 #include "launch.h"
 
@@ -18,25 +18,25 @@ template <int SGS, bool LES>
 cudaError_t run(const StepArgs& a, cudaStream_t st)
 {
     constexpr int S = LBFFS_S;
-    using L = TmaLayout<S>;
+    using L = RingLayout<S>;
     auto kern = k_bulk_tma<S, SGS, LES>;
     // per process: the kernel's shared-memory opt-in and its resident CTAs per SM
     static int per_sm = 0;
     if (per_sm == 0) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::SMEM);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TMA_TW, L::SMEM);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RING_THREADS, L::SMEM);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int tiles_x = (a.nx + TMA_TW - 1) / TMA_TW;
-    const long long ntiles = (long long)tiles_x * a.ny * a.nz;
+    const int tiles_x = (a.nx + RING_TW - 1) / RING_TW;
+    const long long ntiles = (long long)tiles_x * a.ny * a.nz;  // < 2^31: fewer tiles than cells
     long long grid = (long long)nsm * per_sm;
     if (grid > ntiles) grid = ntiles;
-    kern<<<(unsigned)grid, TMA_TW, L::SMEM, st>>>(a, ntiles, tiles_x);
+    kern<<<(unsigned)grid, RING_THREADS, L::SMEM, st>>>(a, (int)ntiles, tiles_x);
     return cudaGetLastError();
 }
 

@@ -1,20 +1,30 @@
-// Row-staged D3Q19 bulk kernel: the pulled rows of a tile reach shared memory by bulk async
-// copies (cp.async.bulk, completion on an mbarrier), the compute threads read them back with
-// fixed shared-memory offsets, and clean tiles leave through bulk async stores.
+// Warp-specialised D3Q19 bulk kernel: a producer warp streams the pulled rows of each tile into
+// a ring of shared-memory stages with bulk async copies (cp.async.bulk, completion counted on an
+// mbarrier), four consumer warps collide the tile's cells from shared memory and store the
+// results (from registers, or for clean 64-cell segments through bulk async stores from a
+// per-warp output buffer: LBFFS_RING_STORE).
 //
-// A tile is TMA_TW consecutive cells of one row (j, k).  Population q of cell x is pulled from
+// A tile is RING_TW consecutive cells of one row (j, k).  Population q of cell x is pulled from
 // x - c_q, so the tile needs, per direction, the row (j - cy, k - cz) over x0 - 1 .. x0 + n: one
 // bulk copy per direction of that row widened to 16-byte boundaries (the padded planes put every
-// row start on a 32-byte sector, so the widened copy is aligned).  Two stages alternate: while
-// the tile of one stage is computed, thread 0 has the next tile's 19 rows in flight.
+// row start on a 32-byte sector, so the widened copy is aligned), plus one copy of the tile's
+// flag bytes.  The producer runs up to NST tiles ahead; a stage is handed back (the "empty"
+// barrier) as soon as every consumer warp has read its inputs, before the collision.
 //
-// A tile whose cells are all plain bulk cells and whose length is a multiple of 16 bytes is
-// written back by 19 bulk stores from a shared-memory output row; any other tile (solid,
-// special, or row-tail cells) has each active thread store its own cell, so cells owned by
+// What this buys over the per-thread kernel: the bytes in flight no longer cost registers and
+// the consumers address shared memory with fixed offsets (no per-direction pointer arithmetic
+// for the loads).  For 2-byte storage a lane owns two adjacent cells, so the two results of a
+// direction are packed into one 32-bit store by one conversion.
+//
+// Only active cells are written: a lane stores its own active cells, and with bulk stores a
+// segment goes through the output buffer only when all its cells are plain bulk cells and its
+// length is a multiple of 16 bytes (others fall back to the lane stores), so cells owned by
 // another kernel or by nobody are never written.
 //
-// Every mbarrier wait is bounded; when a wait runs out, the CTA (deciding together) sets bit 2 of
-// the error word, waits (bounded) for the copies still in flight and leaves the kernel.
+// Every mbarrier wait is bounded and its outcome is taken by the whole warp; when a wait runs
+// out the warp sets bit 2 of the error word and leaves its loop (the other warps' waits then run
+// out in turn), and before the CTA exits the producer waits (bounded) for the copies it still has
+// in flight.  No CTA-wide barrier sits inside the loops.
 #pragma once
 #include <stdint.h>
 
@@ -22,8 +32,28 @@
 
 namespace lbffs {
 
-constexpr int TMA_TW = 128;  // cells per tile = threads per CTA
+constexpr int RING_TW = 256;                      // cells per tile
+constexpr int RING_CW = 4;                        // consumer warps
+constexpr int RING_SEG = RING_TW / RING_CW;       // cells per consumer warp (2 per lane)
+constexpr int RING_THREADS = 32 * (RING_CW + 1);  // consumers + one producer warp
 constexpr unsigned TMA_WAIT_LIMIT = 1u << 20;
+// results: 0 = each lane stores its own cells from registers, 1 = clean 64-cell segments through
+// a per-warp shared-memory buffer and bulk stores (build-time choices, as is the stage count)
+#ifndef LBFFS_RING_STORE
+#define LBFFS_RING_STORE 0
+#endif
+#ifndef LBFFS_RING_NST
+#define LBFFS_RING_NST 0
+#endif
+// resident CTAs per SM the kernel is compiled for (0: the compiler's register choice)
+#ifndef LBFFS_RING_MINB
+#define LBFFS_RING_MINB 6
+#endif
+#if LBFFS_RING_MINB > 0
+#define LBFFS_RING_BOUNDS __launch_bounds__(RING_THREADS, LBFFS_RING_MINB)
+#else
+#define LBFFS_RING_BOUNDS __launch_bounds__(RING_THREADS)
+#endif
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -39,6 +69,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
@@ -114,137 +149,210 @@ __device__ __forceinline__ __nv_bfloat16 held_to<__nv_bfloat16>(float v)
 {
     return __float2bfloat16_rn(v);
 }
+// x components of the D3Q19 directions as bit masks (c_x = +1, c_x = -1)
+__host__ __device__ constexpr unsigned cx_mask19(int s)
+{
+    unsigned m = 0;
+    for (int q = 0; q < 19; q++)
+        if (lat_c(19, q, 0) == s) m |= 1u << q;
+    return m;
+}
 
 template <int S>
-struct TmaLayout {
+struct RingLayout {
     using T = typename Codec<S>::T;
-    static constexpr int E16 = 16 / (int)sizeof(T);           // elements per 16 bytes
-    static constexpr int ROW = TMA_TW + 2 * E16;              // staged elements per direction
-    static constexpr int IN_BYTES = 19 * ROW * (int)sizeof(T);  // one input stage
-    static constexpr int OUT_BYTES = 19 * TMA_TW * (int)sizeof(T);
-    static constexpr int SMEM = 2 * (IN_BYTES + OUT_BYTES) + 64;
+    static constexpr int SZ = (int)sizeof(T);
+    static constexpr bool ADJ = SZ == 2;                // a lane owns cells 2l, 2l + 1 (else l, l + 32)
+    static constexpr int E16 = 16 / SZ;                 // elements per 16 bytes
+    static constexpr int ROW = RING_TW + 2 * E16;       // staged elements per direction
+    static constexpr int NST = LBFFS_RING_NST > 0 ? LBFFS_RING_NST : (SZ == 2 ? 3 : 2);  // input stages
+    static constexpr int IN_BYTES = 19 * ROW * SZ;      // one input stage
+    static constexpr int FL_BYTES = RING_TW + 32;       // a tile's flag bytes, widened to 16 bytes
+    static constexpr int OUT_BYTES = LBFFS_RING_STORE ? 19 * RING_SEG * SZ : 0;  // one consumer warp's output rows
+    static constexpr int OFF_FL = NST * IN_BYTES;
+    static constexpr int OFF_OUT = OFF_FL + NST * FL_BYTES;
+    static constexpr int OFF_HDR = OFF_OUT + RING_CW * OUT_BYTES;
+    static constexpr int OFF_BAR = OFF_HDR + NST * 32;
+    static constexpr int SMEM = OFF_BAR + 2 * NST * 8;
+    static_assert(IN_BYTES % 16 == 0 && OUT_BYTES % 16 == 0 && FL_BYTES % 16 == 0, "16-byte stages");
+};
+
+// tile header written by the producer: first cell, cells, row, offset of the first cell's flag
+// byte in the staged flag bytes
+struct RingHdr {
+    int x0, n, j, k, foff, pad0, pad1, pad2;
 };
 
 template <int S, int SGS, bool LES>
-__global__ void __launch_bounds__(TMA_TW) k_bulk_tma(const StepArgs a, long long ntiles, int tiles_x)
+__global__ void LBFFS_RING_BOUNDS k_bulk_tma(const StepArgs a, int ntiles, int tiles_x)
 {
     using T = typename Codec<S>::T;
-    using L = TmaLayout<S>;
+    using L = RingLayout<S>;
+    constexpr int NST = L::NST, ROW = L::ROW, E16 = L::E16, SZ = L::SZ;
+    constexpr unsigned CXP = cx_mask19(1), CXM = cx_mask19(-1);
     extern __shared__ __align__(128) unsigned char smem[];
-    T* in = reinterpret_cast<T*>(smem);                            // [2][19][ROW]
-    T* out = reinterpret_cast<T*>(smem + 2 * L::IN_BYTES);         // [2][19][TW]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * (L::IN_BYTES + L::OUT_BYTES));
-    const int tid = threadIdx.x;
+    T* in = reinterpret_cast<T*>(smem);                                  // [NST][19][ROW]
+    uint8_t* flb = smem + L::OFF_FL;                                     // [NST][FL_BYTES]
+    T* outb = reinterpret_cast<T*>(smem + L::OFF_OUT);                   // [RING_CW][19][RING_SEG]
+    RingHdr* hdr = reinterpret_cast<RingHdr*>(smem + L::OFF_HDR);        // [NST]
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);     // [NST]
+    uint64_t* empty = full + NST;                                        // [NST]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    // tile -> first cell x0, cells n, row (j, k)
-    auto decode = [&](long long t, int& x0, int& n, int& j, int& k) {
-        const int xb = (int)(t % tiles_x);
-        const long long row = t / tiles_x;
-        j = (int)(row % a.ny);
-        k = (int)(row / a.ny);
-        x0 = xb * TMA_TW;
-        n = min(TMA_TW, a.nx - x0);
-    };
-    // thread 0: the 19 pulled rows of tile t into stage st
-    auto issue = [&](long long t, int st) {
-        int x0, n, j, k;
-        decode(t, x0, n, j, k);
-        const int count = ((n + 1 + L::E16) + L::E16 - 1) / L::E16 * L::E16;  // covers x0 - E16 .. x0 + n
-        const unsigned bytes = (unsigned)count * (unsigned)sizeof(T);
-        mbar_expect_tx(&bar[st], 19u * bytes);
-#pragma unroll
-        for (int q = 0; q < 19; q++) {
-            const T* src = static_cast<const T*>(a.fin_q[q]) +
-                           pidx(a, x0 - L::E16, j - lat_c(19, q, 1), k - lat_c(19, q, 2));
-            bulk_load(in + (st * 19 + q) * L::ROW, src, bytes, &bar[st]);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], RING_CW);
         }
-    };
-
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
         fence_mbar_init();
     }
     __syncthreads();
-    long long tile = blockIdx.x;
-    if (tid == 0 && tile < ntiles) issue(tile, 0);
-    int it = 0;
-    bool failed = false;
-    for (; tile < ntiles; tile += gridDim.x, it++) {
-        const int st = it & 1;
-        const long long next = tile + gridDim.x;
-        // stage st ^ 1 was last read in the previous iteration, which ended with a barrier
-        if (tid == 0 && next < ntiles) issue(next, st ^ 1);
-        // every thread observes the phase itself (acquiring the copied rows); the give-up decision
-        // is taken by the whole CTA together so that no thread is left at a barrier
-        const bool got = mbar_wait(&bar[st], (unsigned)((it >> 1) & 1));
-        if (!__syncthreads_and(got)) {
-            failed = true;
-            break;
+
+    int issued = 0;  // producer: tiles whose copies were issued
+    if (warp == RING_CW) {
+        // ---- producer ----
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, issued++) {
+            const int st = issued % NST, u = issued / NST;
+            // the stage's previous tile has been read by every consumer warp
+            if (u > 0 && !__all_sync(0xffffffffu, mbar_wait(&empty[st], (unsigned)((u - 1) & 1)))) {
+                if (lane == 0 && a.err) atomicOr(a.err, 2);
+                break;
+            }
+            const int row = t / tiles_x;
+            const int x0 = (t - row * tiles_x) * RING_TW;
+            const int j = row % a.ny, k = row / a.ny;
+            const int n = min(RING_TW, a.nx - x0);
+            const int count = (n + 2 * E16) / E16 * E16;  // x0 - E16 .. x0 + n, whole 16-byte units
+            const int fo = row * a.nx + x0;
+            const int fstart = fo & ~15;
+            const int fbytes = ((fo + n + 15) & ~15) - fstart;
+            if (lane == 0) {
+                hdr[st] = RingHdr{x0, n, j, k, fo - fstart, 0, 0, 0};
+                mbar_expect_tx(&full[st], 19u * (unsigned)(count * SZ) + (unsigned)fbytes);
+            }
+            __syncwarp();
+            if (lane < 19) {
+                // row (j - cy, k - cz) from x0 - E16: the pulled plane base moved back by c_x
+                const int cx = (int)((CXP >> lane) & 1u) - (int)((CXM >> lane) & 1u);
+                const T* src = static_cast<const T*>(a.fin_s[lane]) + (pidx(a, x0 - E16, j, k) + cx);
+                bulk_load(in + (st * 19 + lane) * ROW, src, (unsigned)(count * SZ), &full[st]);
+            } else if (lane == 19) {
+                bulk_load(flb + st * L::FL_BYTES, a.flags + fstart, (unsigned)fbytes, &full[st]);
+            }
         }
-        int x0, n, j, k;
-        decode(tile, x0, n, j, k);
-        const bool valid = tid < n;
-        const int i = x0 + tid;
-        const int ic = (k * a.ny + j) * a.nx + i;
-        const uint8_t fl = valid ? __ldg(a.flags + ic) : FL_SOLID;
-        const bool act = !(fl & (FL_SOLID | FL_SPECIAL));
-        const bool clean = __syncthreads_and(!valid || act) && (n % L::E16) == 0;
-        if (act) {
-            const T* row = in + st * 19 * L::ROW + L::E16 + tid;
-            float ft[19];
+    } else {
+        // ---- consumers: lane l of warp w owns cells xi[0], xi[1] of the tile ----
+        const int xi[2] = {L::ADJ ? RING_SEG * warp + 2 * lane : RING_SEG * warp + lane,
+                           L::ADJ ? RING_SEG * warp + 2 * lane + 1 : RING_SEG * warp + lane + 32};
+        T* ob = outb + warp * 19 * RING_SEG;
+        int it = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+            const int st = it % NST, u = it / NST;
+            if (!__all_sync(0xffffffffu, mbar_wait(&full[st], (unsigned)(u & 1)))) {
+                if (lane == 0 && a.err) atomicOr(a.err, 2);
+                break;
+            }
+            const RingHdr h = hdr[st];
+            const uint8_t* fls = flb + st * L::FL_BYTES + h.foff;
+            uint8_t fl[2];
+            bool act[2], valid[2];
+#pragma unroll
+            for (int v = 0; v < 2; v++) {
+                valid[v] = xi[v] < h.n;
+                fl[v] = valid[v] ? fls[xi[v]] : FL_SOLID;
+                act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
+            }
+            const T* r = in + st * 19 * ROW + E16;
+            F2 ft[19];
+#pragma unroll
+            for (int q = 0; q < 19; q++) {
+                const int cx = lat_c(19, q, 0);
+                const T* p = r + q * ROW - cx;
+                if constexpr (L::ADJ) {
+                    if (cx == 0) {
+                        // the two cells' elements are one aligned 32-bit word
+                        ft[q] = held_unpack(T{}, *reinterpret_cast<const uint32_t*>(p + xi[0]));
+                    } else {
+                        ft[q] = pk(held_of(p[xi[0]]), held_of(p[xi[1]]));
+                    }
+                } else {
+                    ft[q] = pk(held_of(p[xi[0]]), held_of(p[xi[1]]));
+                }
+            }
+            // inputs read: hand the stage back to the producer
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+            if (!__any_sync(0xffffffffu, act[0] || act[1])) continue;
+            const int row = h.k * a.ny + h.j;
+            const int ci[2] = {h.x0 + xi[0], h.x0 + xi[1]}, cj[2] = {h.j, h.j}, ck[2] = {h.k, h.k};
+            const int ic[2] = {row * a.nx + ci[0], row * a.nx + ci[1]};
             if constexpr (SGS != SGS_WALE) {
-                // the two-lane collision of the per-thread kernel with the second lane idle, so
-                // both variants round every cell the same way
-                F2 fp[19];
-#pragma unroll
-                for (int q = 0; q < 19; q++) fp[q] = pk(held_of(row[q * L::ROW - lat_c(19, q, 0)]), 0.f);
-                const uint8_t fl2[2] = {fl, FL_SOLID};
-                const bool act2[2] = {true, false};
-                const int ci[2] = {i, i}, cj[2] = {j, j}, ck[2] = {k, k}, ic2[2] = {ic, ic};
-                bulk_collide2<S, LES>(a, fp, fl2, act2, ci, cj, ck, ic2);
-#pragma unroll
-                for (int q = 0; q < 19; q++) ft[q] = lane0(fp[q]);
+                bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic);
             } else {
+                // WALE: the scalar path, one cell at a time
 #pragma unroll
-                for (int q = 0; q < 19; q++) ft[q] = held_of(row[q * L::ROW - lat_c(19, q, 0)]);
-                bulk_collide<19, S, COLL_RR, SGS, LES>(a, ft, fl, i, j, k, ic);
+                for (int v = 0; v < 2; v++) {
+                    float fs[19];
+#pragma unroll
+                    for (int q = 0; q < 19; q++) fs[q] = v == 0 ? lane0(ft[q]) : lane1(ft[q]);
+                    if (act[v]) bulk_collide<19, S, COLL_RR, SGS, LES>(a, fs, fl[v], ci[v], h.j, h.k, ic[v]);
+#pragma unroll
+                    for (int q = 0; q < 19; q++) ft[q] = v == 0 ? pk(fs[q], lane1(ft[q])) : pk(lane0(ft[q]), fs[q]);
+                }
             }
+            const int m = min(max(h.n - RING_SEG * warp, 0), RING_SEG);
+            const bool ok = (!valid[0] || act[0]) && (!valid[1] || act[1]);
+            const bool clean = LBFFS_RING_STORE && __all_sync(0xffffffffu, ok) && (m * SZ) % 16 == 0;
             if (clean) {
-                T* o = out + st * 19 * TMA_TW + tid;
+                // this warp's previous bulk stores have read the output buffer
+                if (lane < 19) bulk_wait_read<0>();
+                __syncwarp();
 #pragma unroll
-                for (int q = 0; q < 19; q++) o[q * TMA_TW] = held_to<T>(ft[q]);
+                for (int q = 0; q < 19; q++) {
+                    if constexpr (L::ADJ)
+                        reinterpret_cast<uint32_t*>(ob + q * RING_SEG)[lane] = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
+                    else {
+                        ob[q * RING_SEG + lane] = held_to<T>(lane0(ft[q]));
+                        ob[q * RING_SEG + lane + 32] = held_to<T>(lane1(ft[q]));
+                    }
+                }
+                fence_async_smem();
+                __syncwarp();
+                if (lane < 19) {
+                    T* dst = static_cast<T*>(a.fout_q[lane]) + pidx(a, h.x0 + RING_SEG * warp, h.j, h.k);
+                    bulk_store(dst, ob + lane * RING_SEG, (unsigned)(m * SZ));
+                    bulk_commit();
+                }
             } else {
-                const int ip = pidx(a, i, j, k);
+                const int ip[2] = {pidx(a, ci[0], h.j, h.k), pidx(a, ci[1], h.j, h.k)};
+                // adjacent 2-byte cells, both active: one 32-bit store (ip[0] is even: every row
+                // starts on a 32-byte sector and the pair on an even cell)
+                const bool both = L::ADJ && act[0] && act[1];
 #pragma unroll
-                for (int q = 0; q < 19; q++) Codec<S>::store_held(static_cast<T*>(a.fout_q[q]) + ip, ft[q]);
+                for (int q = 0; q < 19; q++) {
+                    T* p = static_cast<T*>(a.fout_q[q]);
+                    if constexpr (L::ADJ) {
+                        if (both) {
+                            *reinterpret_cast<uint32_t*>(p + ip[0]) = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
+                            continue;
+                        }
+                    }
+                    if (act[0]) Codec<S>::store_held(p + ip[0], lane0(ft[q]));
+                    if (act[1]) Codec<S>::store_held(p + ip[1], lane1(ft[q]));
+                }
             }
         }
-        // each writer orders its shared-memory stores before the bulk stores that read them
-        if (clean) fence_async_smem();
-        __syncthreads();  // output rows of stage st written; input stage st fully read
-        if (tid == 0) {
-            if (clean) {
-                const int ip0 = pidx(a, x0, j, k);
-                const unsigned bytes = (unsigned)n * (unsigned)sizeof(T);
-#pragma unroll
-                for (int q = 0; q < 19; q++)
-                    bulk_store(static_cast<T*>(a.fout_q[q]) + ip0, out + (st * 19 + q) * TMA_TW, bytes);
-            }
-            bulk_commit();
-            bulk_wait_read<1>();  // the previous iteration's output stage may be rewritten
-        }
-        __syncthreads();
+        if (LBFFS_RING_STORE && lane < 19) bulk_wait_all();
     }
-    if (failed) {
-        if (tid == 0) {
-            if (a.err) atomicOr(a.err, 2);
-            // the next tile's rows may still be in flight into this CTA's shared memory
-            const long long next = tile + gridDim.x;
-            if (next < ntiles) mbar_wait(&bar[(it & 1) ^ 1], (unsigned)(((it + 1) >> 1) & 1));
+    __syncthreads();
+    // copies still in flight into this CTA's shared memory (only after a wait ran out): the last
+    // tile issued into each stage has landed
+    if (warp == RING_CW && lane == 0) {
+        for (int s = 0; s < NST && s < issued; s++) {
+            const int u_last = (issued - 1 - s) / NST;
+            if (!mbar_wait(&full[s], (unsigned)(u_last & 1)) && a.err) atomicOr(a.err, 2);
         }
     }
-    if (tid == 0) bulk_wait_all();
 }
 
 }  // namespace lbffs

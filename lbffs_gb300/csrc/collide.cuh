@@ -167,24 +167,29 @@ __device__ __forceinline__ Mom19T<V> moments19(const V (&f)[19])
 template <int HS = 1, class V = float>
 __device__ __forceinline__ V smag_pp19(const Mom19T<V>& m, V u, V v, V w)
 {
+    // each component is formed with its sign flipped (u_a u_b minus the moment), which the squares
+    // below do not see; the products are fused explicitly
     const V r3 = m.r * (1.f / 3.f);
     V pxx, pyy, pzz, pxy, pxz, pyz;
     if constexpr (HS == 1) {
-        pxx = m.s[0][0] - r3 - u * u, pyy = m.s[1][1] - r3 - v * v, pzz = m.s[2][2] - r3 - w * w;
-        pxy = m.s[0][1] - u * v, pxz = m.s[0][2] - u * w, pyz = m.s[1][2] - v * w;
+        pxx = mad(u, u, r3 - m.s[0][0]), pyy = mad(v, v, r3 - m.s[1][1]), pzz = mad(w, w, r3 - m.s[2][2]);
+        pxy = mad(u, v, neg(m.s[0][1])), pxz = mad(u, w, neg(m.s[0][2])), pyz = mad(v, w, neg(m.s[1][2]));
     } else {
         constexpr float is = 1.f / HS;
-        pxx = (m.s[0][0] - r3) * is - u * u, pyy = (m.s[1][1] - r3) * is - v * v, pzz = (m.s[2][2] - r3) * is - w * w;
-        pxy = m.s[0][1] * is - u * v, pxz = m.s[0][2] * is - u * w, pyz = m.s[1][2] * is - v * w;
+        pxx = mad(u, u, (r3 - m.s[0][0]) * is), pyy = mad(v, v, (r3 - m.s[1][1]) * is);
+        pzz = mad(w, w, (r3 - m.s[2][2]) * is);
+        pxy = mad(u, v, m.s[0][1] * (-is)), pxz = mad(u, w, m.s[0][2] * (-is)), pyz = mad(v, w, m.s[1][2] * (-is));
     }
-    return pxx * pxx + pyy * pyy + pzz * pzz + 2.f * (pxy * pxy + pxz * pxz + pyz * pyz);
+    V t = mad(pyz, pyz, mad(pxz, pxz, pxy * pxy));
+    t = t + t;
+    return mad(pxx, pxx, mad(pyy, pyy, mad(pzz, pzz, t)));
 }
 
 // the eddy relaxation time of smagorinskyTauSGS (without damping) from Pi_neq : Pi_neq
 __device__ __forceinline__ float smag_tau(float pp, float rho, float omega, float les, float cs)
 {
     const float tau = 1.f / omega;
-    return les * 0.5f * (-tau + sqrtf(tau * tau + 18.f * 1.41421356237f * cs * cs * sqrtf(pp) / rho));
+    return les * 0.5f * (sqrtf(fmaf(tau, tau, 18.f * 1.41421356237f * cs * cs * sqrtf(pp) / rho)) - tau);
 }
 
 template <int HS = 1>
@@ -202,26 +207,33 @@ template <int HS = 1, class V = float>
 __device__ __forceinline__ void collide_rr19m(V (&f)[19], const Mom19T<V>& m, const V (&U)[3], V we, V ir1,
                                               float omega_b, float dpdx)
 {
+    // every multiply that feeds an add is fused explicitly (mad)
     const float third = 1.f / 3.f;
-    const V k1 = 1.f - we, rho = m.rho;
-    const V ir = ir1 * (1.f / HS);
+    const V k1 = 1.f - we, rho = m.rho, nwe = neg(we);
+    V ir;
+    if constexpr (HS == 1) ir = ir1;
+    else ir = ir1 * (1.f / HS);
     const V r3 = m.r * third;
+    const V NU[3] = {neg(U[0]), neg(U[1]), neg(U[2])};
+    const V UU[3] = {U[0] * U[0], U[1] * U[1], U[2] * U[2]};
+    const V U2[3] = {U[0] + U[0], U[1] + U[1], U[2] + U[2]};
+    const V TU[3] = {U[0] * third, U[1] * third, U[2] * third};
     V N2[3][3], R2[3][3];
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int b = a; b < 3; b++) {
             const V m2 = (a == b) ? (m.s[a][a] - r3) * ir : m.s[a][b] * ir;
-            N2[a][b] = N2[b][a] = m2 - U[a] * U[b];
+            N2[a][b] = N2[b][a] = mad(NU[a], U[b], m2);
             R2[a][b] = R2[b][a] = m2;
         }
     const V wm = (omega_b - we) * third;
-    const V nsum = N2[0][0] + N2[1][1] + N2[2][2];
+    const V wn = wm * (N2[0][0] + N2[1][1] + N2[2][2]);
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        R2[a][a] -= wm * nsum + we * N2[a][a];  // omega_P on the own axis, omega_M on the others
+        R2[a][a] = R2[a][a] - mad(we, N2[a][a], wn);  // omega_P on the own axis, omega_M on the others
 #pragma unroll
-        for (int b = a + 1; b < 3; b++) R2[a][b] = R2[b][a] = R2[a][b] - we * N2[a][b];
+        for (int b = a + 1; b < 3; b++) R2[a][b] = R2[b][a] = mad(nwe, N2[a][b], R2[a][b]);
     }
     // T3[a][b]: c_a^2 c_b moment; Q4[a][b]: c_a^2 c_b^2 moment minus its constant 1/9
     V T3[3][3], Q4[3][3];
@@ -230,10 +242,11 @@ __device__ __forceinline__ void collide_rr19m(V (&f)[19], const Mom19T<V>& m, co
 #pragma unroll
         for (int b = 0; b < 3; b++) {
             if (a == b) continue;
-            T3[a][b] = U[a] * U[a] * U[b] + k1 * (U[b] * N2[a][a] + 2.f * U[a] * N2[a][b]) + third * U[b];
+            const V n3 = mad(U[b], N2[a][a], U2[a] * N2[a][b]);
+            T3[a][b] = mad(UU[a], U[b], mad(k1, n3, TU[b]));
             if (b > a) {
-                const V n4 = U[b] * U[b] * N2[a][a] + U[a] * U[a] * N2[b][b] + 4.f * U[a] * U[b] * N2[a][b];
-                Q4[a][b] = Q4[b][a] = U[a] * U[a] * U[b] * U[b] + k1 * n4 + third * (R2[a][a] + R2[b][b]);
+                const V n4 = mad(UU[b], N2[a][a], mad(UU[a], N2[b][b], (U2[a] * U2[b]) * N2[a][b]));
+                Q4[a][b] = Q4[b][a] = mad(UU[a], UU[b], mad(k1, n4, (R2[a][a] + R2[b][b]) * third));
             }
         }
     const V h = rho * (0.5f * HS), qr = rho * (0.25f * HS);
@@ -243,7 +256,7 @@ __device__ __forceinline__ void collide_rr19m(V (&f)[19], const Mom19T<V>& m, co
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const int b = (a + 1) % 3, d = (a + 2) % 3;
-        const V A = base1 + h * (R2[a][a] - Q4[a][b] - Q4[a][d]);
+        const V A = mad(h, R2[a][a] - Q4[a][b] - Q4[a][d], base1);
         const V B = h * (U[a] - T3[b][a] - T3[d][a]);
         if (a == 0) {
             f[1] = A + B + src1;
@@ -257,7 +270,7 @@ __device__ __forceinline__ void collide_rr19m(V (&f)[19], const Mom19T<V>& m, co
 #pragma unroll
     for (int p = 0; p < 3; p++) {
         const int a = p < 2 ? 0 : 1, b = p == 0 ? 1 : 2;
-        const V P = base2 + qr * Q4[a][b], Rr = qr * R2[a][b], X = qr * T3[a][b], Y = qr * T3[b][a];
+        const V P = mad(qr, Q4[a][b], base2), Rr = qr * R2[a][b], X = qr * T3[a][b], Y = qr * T3[b][a];
         const V pp = P + Rr, pm = P - Rr, xp = X + Y, xm = Y - X;
         if (a == 0) {
             f[7 + 4 * p] = pp + xp + src2;

@@ -204,7 +204,8 @@ __device__ __forceinline__ bool in_box(const StepArgs& a, int i, int j, int k)
     return i >= b[0] && i <= b[3] && j >= b[1] && j <= b[4] && k >= b[2] && k <= b[5];
 }
 
-// tauSpongeZone (D3Q19 kernel.cl:2444-2503)
+// tauSpongeZone (D3Q19 kernel.cl:2444-2503); the blend is fused explicitly so that its rounding
+// does not depend on the code around it
 __device__ __forceinline__ float sponge_tau(const StepArgs& a, float tau, float tsgs, int i, int j, int k)
 {
     if (a.sponge_mask == 0) return tau;
@@ -216,13 +217,13 @@ __device__ __forceinline__ float sponge_tau(const StepArgs& a, float tau, float 
         if ((a.sponge_mask >> (2 * d)) & 1) {
             if ((float)x[d] < n * a.spz) {
                 const float fx = (float)x[d] / (n * a.spz);
-                tau = (1.f - fx) * (1.f - tsgs) + fx * tau;
+                tau = fmaf(fx, tau, (1.f - fx) * (1.f - tsgs));
             }
         }
         if ((a.sponge_mask >> (2 * d + 1)) & 1) {
             if ((float)x[d] > n * (1.f - a.spz)) {
                 const float fx = (float)(N[d] - x[d]) / (n * a.spz);
-                tau = (1.f - fx) * (1.f - tsgs) + fx * tau;
+                tau = fmaf(fx, tau, (1.f - fx) * (1.f - tsgs));
             }
         }
     }

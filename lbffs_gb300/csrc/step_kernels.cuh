@@ -28,6 +28,11 @@ constexpr int SPECIAL_BS = 128;
 // CTAs ahead whose pulled rows a 2-byte D3Q19 bulk CTA prefetches into L2 (0: none); a build-time
 // tuning value.  608 (half a wave of 8-CTA-per-SM residency) measured 4 % faster on the 256^3
 // FP16S / BF16S cavity than none or 304, the same as 1216.
+// 2-byte D3Q19 bulk cells: a lane owns two adjacent cells (1) or two cells 32 apart (0); a
+// build-time choice
+#ifndef LBFFS_BULK_ADJ
+#define LBFFS_BULK_ADJ 1
+#endif
 #ifndef LBFFS_BULK_PREFETCH
 #define LBFFS_BULK_PREFETCH 608
 #endif
@@ -244,7 +249,8 @@ __device__ __forceinline__ void bulk_collide(const StepArgs& a, float (&ft)[Q], 
         rho = m.rho;
         const float ir = 1.f / rho;
         const float irs = ir * (1.f / HS);
-        u = m.j[0] * irs + 0.5f * a.dpdx * ir;  // updateRhoUVW (kernel.cl:3509-3523)
+        const float hd = ir * (0.5f * a.dpdx);
+        u = fmaf(m.j[0], irs, hd);  // updateRhoUVW (kernel.cl:3509-3523)
         v = m.j[1] * irs;
         w = m.j[2] * irs;
         if constexpr (SGS == SGS_WALE) {
@@ -264,7 +270,7 @@ __device__ __forceinline__ void bulk_collide(const StepArgs& a, float (&ft)[Q], 
             a.w_n[ic] = w;
             a.tau_n[ic] = tsgs;
         }
-        const float U[3] = {u - 0.5f * a.dpdx * ir, v, w};
+        const float U[3] = {u - hd, v, w};
         collide_rr19m<HS>(ft, m, U, we, ir, a.omega_b, a.dpdx);
     } else if constexpr (SGS != SGS_WALE) {
         // D3Q27: one pass over the 13 opposite pairs gives rho, j and the second moments that both
@@ -345,8 +351,11 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], c
         irl[v] = 1.f / lane(m.rho, v);
     }
     const F2 ir = pk(irl[0], irl[1]);
-    const F2 irs = ir * (1.f / HS);
-    const F2 u = m.j[0] * irs + (0.5f * a.dpdx) * ir;  // updateRhoUVW (kernel.cl:3509-3523)
+    F2 irs;
+    if constexpr (HS == 1) irs = ir;
+    else irs = ir * (1.f / HS);
+    const F2 hd = ir * (0.5f * a.dpdx);
+    const F2 u = mad(m.j[0], irs, hd);  // updateRhoUVW (kernel.cl:3509-3523)
     const F2 v = m.j[1] * irs;
     const F2 w = m.j[2] * irs;
     float tsl[2] = {0.f, 0.f}, wel[2];
@@ -372,7 +381,7 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], c
         const float tau = sponge_tau(a, 1.f / oml[c], tsl[c], ci[c], cj[c], ck[c]);
         wel[c] = 1.f / (tau + tsl[c]);
     }
-    const F2 U[3] = {u - (0.5f * a.dpdx) * ir, v, w};
+    const F2 U[3] = {u - hd, v, w};
     collide_rr19m<HS>(ft, m, U, pk(wel[0], wel[1]), ir, a.omega_b, a.dpdx);
 }
 
@@ -400,6 +409,73 @@ __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)
     }
 }
 
+// two held values as one 32-bit word of 2-byte elements, x in the low half (each element
+// rounded exactly as held_to rounds it)
+__device__ __forceinline__ uint32_t held_pack(__half, float x, float y)
+{
+    const __half2 h = __floats2half2_rn(x, y);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ uint32_t held_pack(__nv_bfloat16, float x, float y)
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x, y);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// a 32-bit word of two 2-byte elements as held values (low half in lane 0)
+__device__ __forceinline__ F2 held_unpack(__half, uint32_t wd)
+{
+    __half2 h;
+    memcpy(&h, &wd, 4);
+    return pk(__low2float(h), __high2float(h));
+}
+__device__ __forceinline__ F2 held_unpack(__nv_bfloat16, uint32_t wd)
+{
+    __nv_bfloat162 h;
+    memcpy(&h, &wd, 4);
+    return pk(__low2float(h), __high2float(h));
+}
+
+// bulk_pair for two adjacent cells of 2-byte storage (ip0 even, cell ip0 + 1 the second): the
+// pulls with c_x = 0 of both cells are one aligned 32-bit word (the pull offset c_y px + c_z pxy is
+// even), and when both cells are active their results leave as one packed 32-bit store.  Both
+// cells' pulls are read when either is active (the row is padded by a ghost cell on each side).
+template <int S, bool LES>
+__device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
+                                              const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
+                                              const int (&ic)[2], int ip0)
+{
+    using T = typename Codec<S>::T;
+    static_assert(sizeof(T) == 2, "2-byte storage");
+    const bool any = act[0] || act[1];
+    F2 ft[19];
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        const T* p = static_cast<const T*>(a.fin_s[q]) + ip0;
+        if (lat_c(19, q, 0) == 0) {
+            const uint32_t wd = any ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
+            ft[q] = held_unpack(T{}, wd);
+        } else {
+            const float x0 = any ? Codec<S>::load_held(p) : 0.f;
+            const float x1 = any ? Codec<S>::load_held(p + 1) : 0.f;
+            ft[q] = pk(x0, x1);
+        }
+    }
+    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic);
+    if (act[0] && act[1]) {
+#pragma unroll
+        for (int q = 0; q < 19; q++)
+            *reinterpret_cast<uint32_t*>(static_cast<T*>(a.fout_q[q]) + ip0) = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; q++) {
+            T* p = static_cast<T*>(a.fout_q[q]) + ip0;
+            if (act[0]) Codec<S>::store_held(p, lane0(ft[q]));
+            if (act[1]) Codec<S>::store_held(p + 1, lane1(ft[q]));
+        }
+    }
+}
+
 // One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
 // instruction of a warp covers 32 consecutive cells.  Every population is pulled from the same
 // offset for every cell: cells on the domain border read the ghost layer, which k_halo filled
@@ -411,8 +487,13 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     using T = typename Codec<S>::T;
     constexpr bool HELD = (Q == 19);
     constexpr int V = bulk_v<Q>();
+    // 2-byte D3Q19 pair path: a lane owns two adjacent cells (bulk_pair_adj); otherwise cells
+    // lane + 32 v
+    constexpr bool ADJ = Q == 19 && SGS != SGS_WALE && V == 2 && S != ST_FP32 && LBFFS_BULK_ADJ;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i0 = (xb * (BULK_BX / 32) + warp) * (32 * V) + lane;
+    const int base = (xb * (BULK_BX / 32) + warp) * (32 * V);
+    const int i0 = ADJ ? base + 2 * lane : base + lane;
+    constexpr int DV = ADJ ? 1 : 32;  // x distance of a lane's consecutive cells
     const int row = (k * a.ny + j) * a.nx;
     const int prow = pidx(a, 0, j, k);
     uint8_t fl[V];
@@ -420,7 +501,7 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     bool any = false;
 #pragma unroll
     for (int v = 0; v < V; v++) {
-        const int i = i0 + 32 * v;
+        const int i = i0 + DV * v;
         fl[v] = (i < a.nx) ? __ldg(a.flags + row + i) : FL_SOLID;
         act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
         any |= act[v];
@@ -448,7 +529,11 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         }
     }
 #endif
-    if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) {
+    if constexpr (ADJ) {
+        const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
+        const int ic[2] = {row + i0, row + i0 + 1};
+        bulk_pair_adj<S, LES>(a, fl, act, ci, cj, ck, ic, prow + i0);
+    } else if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) {
         const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
         bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
@@ -457,7 +542,7 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
 #pragma unroll
         for (int v = 0; v < V; v++) {
             if (!act[v]) continue;
-            const int ip = prow + i0 + 32 * v;
+            const int ip = prow + i0 + DV * v;
 #pragma unroll
             for (int q = 0; q < Q; q++) {
                 const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
@@ -467,7 +552,7 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
 #pragma unroll
         for (int v = 0; v < V; v++) {
             if (!act[v]) continue;
-            const int i = i0 + 32 * v;
+            const int i = i0 + DV * v;
             bulk_cell<Q, S, COLL, SGS, LES>(a, ft[v], fl[v], i, j, k, row + i, prow + i);
         }
     }
