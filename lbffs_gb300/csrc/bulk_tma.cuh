@@ -287,7 +287,8 @@ __global__ void LBFFS_RING_BOUNDS k_bulk_tma(const StepArgs a, int ntiles, int t
             const int ci[2] = {h.x0 + xi[0], h.x0 + xi[1]}, cj[2] = {h.j, h.j}, ck[2] = {h.k, h.k};
             const int ic[2] = {row * a.nx + ci[0], row * a.nx + ci[1]};
             if constexpr (SGS != SGS_WALE) {
-                bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic);
+                const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
+                bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
             } else {
                 // WALE: the scalar path, one cell at a time
 #pragma unroll

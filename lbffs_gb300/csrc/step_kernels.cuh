@@ -333,21 +333,31 @@ __device__ __forceinline__ void bulk_cell(const StepArgs& a, float (&ft)[Q], uin
     }
 }
 
+// the per-lane test of bulk_collide2's plain path (the caller takes it over the whole warp)
+__device__ __forceinline__ bool plain_pair(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2])
+{
+    return act[0] && act[1] && !((fl[0] | fl[1]) & (FL_OMEGA | FL_SDF | FL_STORE)) && !a.store_all && !a.ibm_box &&
+           a.sponge_mask == 0;
+}
+
 // bulk_collide for the two cells of a thread at once (D3Q19, Smagorinsky or no SGS): the moments,
 // the velocity and the recursive regularised collision run on packed FP32x2 lanes (lane v = cell
 // v); the per-cell parts (relaxation rates, eddy viscosity square roots, sponge, field stores)
 // run per lane.  act[v]: cell v is a bulk cell (the other lane's values are computed and dropped).
+// plain (the same for the whole warp, see plain_pair): both cells active, uniform omega, no wall
+// damping, no field stores and no sponge, so the per-lane part reduces to the relaxation rates;
+// it computes the same numbers as the general path.
 template <int S, bool LES>
 __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], const uint8_t (&fl)[2],
                                               const bool (&act)[2], const int (&ci)[2], const int (&cj)[2],
-                                              const int (&ck)[2], const int (&ic)[2])
+                                              const int (&ck)[2], const int (&ic)[2], bool plain = false)
 {
     constexpr int HS = Codec<S>::HS;
     const Mom19T<F2> m = moments19<Codec<S>::DEV, HS>(ft);
     float irl[2], oml[2];
 #pragma unroll
     for (int v = 0; v < 2; v++) {
-        oml[v] = (fl[v] & FL_OMEGA) ? __ldg(a.omega + ic[v]) : a.omega0;
+        oml[v] = (!plain && (fl[v] & FL_OMEGA)) ? __ldg(a.omega + ic[v]) : a.omega0;
         irl[v] = 1.f / lane(m.rho, v);
     }
     const F2 ir = pk(irl[0], irl[1]);
@@ -361,6 +371,15 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], c
     float tsl[2] = {0.f, 0.f}, wel[2];
     F2 pp;
     if constexpr (LES) pp = smag_pp19<HS>(m, u, v, w);
+    if (plain) {
+        const float tau0 = 1.f / a.omega0;
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+            if constexpr (LES) tsl[c] = smag_tau(lane(pp, c), lane(m.rho, c), a.omega0, a.les, a.cs);
+            wel[c] = 1.f / (tau0 + tsl[c]);
+        }
+        if (a.err && !(lane0(m.rho) == lane0(m.rho) && lane1(m.rho) == lane1(m.rho))) atomicOr(a.err, 1);
+    } else
 #pragma unroll
     for (int c = 0; c < 2; c++) {
         const float rho = lane(m.rho, c);
@@ -389,7 +408,7 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], c
 template <int S, bool LES>
 __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                           const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
-                                          const int (&ic)[2], const int (&ip)[2])
+                                          const int (&ic)[2], const int (&ip)[2], bool plain = false)
 {
     using T = typename Codec<S>::T;
     F2 ft[19];
@@ -400,7 +419,7 @@ __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)
         const float x1 = act[1] ? Codec<S>::load_held(p + ip[1]) : 0.f;
         ft[q] = pk(x0, x1);
     }
-    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic);
+    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
 #pragma unroll
     for (int q = 0; q < 19; q++) {
         T* p = static_cast<T*>(a.fout_q[q]);
@@ -443,7 +462,7 @@ __device__ __forceinline__ F2 held_unpack(__nv_bfloat16, uint32_t wd)
 template <int S, bool LES>
 __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                               const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
-                                              const int (&ic)[2], int ip0)
+                                              const int (&ic)[2], int ip0, bool plain = false)
 {
     using T = typename Codec<S>::T;
     static_assert(sizeof(T) == 2, "2-byte storage");
@@ -461,7 +480,7 @@ __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (
             ft[q] = pk(x0, x1);
         }
     }
-    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic);
+    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
     if (act[0] && act[1]) {
 #pragma unroll
         for (int q = 0; q < 19; q++)
@@ -506,6 +525,8 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
         any |= act[v];
     }
+    bool plain = false;
+    if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
     if (!any) return;
 #if LBFFS_BULK_PREFETCH > 0
     // 2-byte D3Q19 storage: L2 prefetch of the rows the CTA LBFFS_BULK_PREFETCH launches ahead
@@ -532,11 +553,11 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     if constexpr (ADJ) {
         const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 1};
-        bulk_pair_adj<S, LES>(a, fl, act, ci, cj, ck, ic, prow + i0);
+        bulk_pair_adj<S, LES>(a, fl, act, ci, cj, ck, ic, prow + i0, plain);
     } else if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) {
         const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
-        bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
+        bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip, plain);
     } else {
         float ft[V][Q];
 #pragma unroll
@@ -567,6 +588,9 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
 {
     using T = typename Codec<S>::T;
     constexpr bool HELD = (Q == 19);
+    // 2-byte D3Q19 pair path: lanes 0-15 own adjacent cell pairs of the warp's first segment,
+    // lanes 16-31 of its second (bulk_pair_adj); otherwise lane l takes cell l of both segments
+    constexpr bool ADJ = Q == 19 && SGS != SGS_WALE && BULK_V == 2 && S != ST_FP32 && LBFFS_BULK_ADJ;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int ci[BULK_V], cj[BULK_V], ck[BULK_V];
     uint8_t fl[BULK_V];
@@ -574,20 +598,25 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
     bool any = false;
 #pragma unroll
     for (int v = 0; v < BULK_V; v++) {
-        const int g = g0 + warp * BULK_V + v;
+        const int g = ADJ ? g0 + warp * BULK_V + (lane >> 4) : g0 + warp * BULK_V + v;
         const int row = g / spr;
-        ci[v] = (g - row * spr) * 32 + lane;
+        ci[v] = ADJ ? (g - row * spr) * 32 + 2 * (lane & 15) + v : (g - row * spr) * 32 + lane;
         cj[v] = row % a.ny;
         ck[v] = row / a.ny;
         fl[v] = (g < nseg && ci[v] < a.nx) ? __ldg(a.flags + (long long)row * a.nx + ci[v]) : FL_SOLID;
         act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
         any |= act[v];
     }
+    bool plain = false;
+    if constexpr (Q == 19 && SGS != SGS_WALE && BULK_V == 2) plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
     if (!any) return;
-    if constexpr (Q == 19 && SGS != SGS_WALE && BULK_V == 2) {
+    if constexpr (ADJ) {
+        const int ic[2] = {(ck[0] * a.ny + cj[0]) * a.nx + ci[0], (ck[0] * a.ny + cj[0]) * a.nx + ci[0] + 1};
+        bulk_pair_adj<S, LES>(a, fl, act, ci, cj, ck, ic, pidx(a, ci[0], cj[0], ck[0]), plain);
+    } else if constexpr (Q == 19 && SGS != SGS_WALE && BULK_V == 2) {
         const int ic[2] = {(ck[0] * a.ny + cj[0]) * a.nx + ci[0], (ck[1] * a.ny + cj[1]) * a.nx + ci[1]};
         const int ip[2] = {pidx(a, ci[0], cj[0], ck[0]), pidx(a, ci[1], cj[1], ck[1])};
-        bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip);
+        bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip, plain);
     } else {
         float ft[BULK_V][Q];
 #pragma unroll
