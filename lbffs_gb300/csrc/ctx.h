@@ -21,6 +21,7 @@ struct lbffs_ctx {
     long long E = 0;
     size_t tsize = 4;
     int nsm = 0;
+    long long l2_bytes = 0;  // the device's L2 size
     cudaStream_t stream = nullptr;
     std::string err = "no error";
 

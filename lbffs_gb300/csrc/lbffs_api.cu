@@ -207,6 +207,9 @@ int lbffs::ctx_create(const lbffs_desc* desc, Arena* arena, cudaStream_t stream,
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d.device);
     c->nsm = nsm > 0 ? nsm : 1;
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, d.device);
+    c->l2_bytes = l2;
 #define CKC(call)                                                                                          \
     do {                                                                                                   \
         cudaError_t e_ = (call);                                                                           \
@@ -572,6 +575,7 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
     a.tau_n = mn[4];
     a.store_all = p->store_fields == 2;
     a.bulk_kind = c->Q == 19 ? c->bulk_kind : 0;
+    a.l2_first = 2LL * c->Q * c->pg.pE * c->tsize <= c->l2_bytes;
 }
 
 extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)

@@ -33,6 +33,18 @@ constexpr int SPECIAL_BS = 128;
 #ifndef LBFFS_BULK_ADJ
 #define LBFFS_BULK_ADJ 1
 #endif
+// L2 eviction priority of the 2-byte bulk pair path's pulls and stores: with LBFFS_BULK_EVICT 1
+// they carry an L2 policy, evict-first when both population copies fit in L2 (StepArgs::l2_first:
+// the boundary kernel's scattered accesses then stay cached; 1024x256x4 FP16S cylinder channel
+// +22 % MLUPS) and evict-normal otherwise (on a 256^3 lattice evict-first measured 11 % slower:
+// adjacent warps' shared sectors were evicted before their second read).  The ghost fill's
+// accesses with LBFFS_HALO_KEEP 1 are evict-last (measured no better).  Build-time choices.
+#ifndef LBFFS_BULK_EVICT
+#define LBFFS_BULK_EVICT 1
+#endif
+#ifndef LBFFS_HALO_KEEP
+#define LBFFS_HALO_KEEP 0
+#endif
 #ifndef LBFFS_BULK_PREFETCH
 #define LBFFS_BULK_PREFETCH 608
 #endif
@@ -455,36 +467,103 @@ __device__ __forceinline__ F2 held_unpack(__nv_bfloat16, uint32_t wd)
     return pk(__low2float(h), __high2float(h));
 }
 
+// global accesses with an L2 cache policy (createpolicy): loads through the non-coherent path
+__device__ __forceinline__ uint64_t l2_policy_evict_first()
+{
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_normal()
+{
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last()
+{
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint32_t ld_hint_b32(const void* p, uint64_t pol)
+{
+    uint32_t v;
+    asm("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ uint16_t ld_hint_b16(const void* p, uint64_t pol)
+{
+    unsigned short v;
+    asm("ld.global.nc.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void st_hint_b32(void* p, uint32_t v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint_b16(void* p, uint16_t v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.b16 [%0], %1, %2;" ::"l"(p), "h"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint_v4(void* p, uint4 v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.v4.b32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w), "l"(pol)
+                 : "memory");
+}
+// a stored 2-byte element (its bits) as the held value
+__device__ __forceinline__ float held_bits(__half, uint16_t b) { return __half2float(__ushort_as_half(b)); }
+__device__ __forceinline__ float held_bits(__nv_bfloat16, uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+
 // bulk_pair for two adjacent cells of 2-byte storage (ip0 even, cell ip0 + 1 the second): the
 // pulls with c_x = 0 of both cells are one aligned 32-bit word (the pull offset c_y px + c_z pxy is
 // even), and when both cells are active their results leave as one packed 32-bit store.  Both
 // cells' pulls are read when either is active (the row is padded by a ghost cell on each side).
-template <int S, bool LES>
-__device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
-                                              const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
-                                              const int (&ic)[2], int ip0, bool plain = false)
+// the 19 pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol
+template <int S>
+__device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool any, [[maybe_unused]] uint64_t pol,
+                                              F2 (&ft)[19])
 {
     using T = typename Codec<S>::T;
     static_assert(sizeof(T) == 2, "2-byte storage");
-    const bool any = act[0] || act[1];
-    F2 ft[19];
 #pragma unroll
     for (int q = 0; q < 19; q++) {
         const T* p = static_cast<const T*>(a.fin_s[q]) + ip0;
         if (lat_c(19, q, 0) == 0) {
-            const uint32_t wd = any ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
+            uint32_t wd = 0u;
+            if constexpr (LBFFS_BULK_EVICT) wd = any ? ld_hint_b32(p, pol) : 0u;
+            else wd = any ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
             ft[q] = held_unpack(T{}, wd);
         } else {
-            const float x0 = any ? Codec<S>::load_held(p) : 0.f;
-            const float x1 = any ? Codec<S>::load_held(p + 1) : 0.f;
+            float x0, x1;
+            if constexpr (LBFFS_BULK_EVICT) {
+                x0 = any ? held_bits(T{}, ld_hint_b16(p, pol)) : 0.f;
+                x1 = any ? held_bits(T{}, ld_hint_b16(p + 1, pol)) : 0.f;
+            } else {
+                x0 = any ? Codec<S>::load_held(p) : 0.f;
+                x1 = any ? Codec<S>::load_held(p + 1) : 0.f;
+            }
             ft[q] = pk(x0, x1);
         }
     }
-    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+}
+
+// the results of two adjacent cells at ip0: one packed 32-bit store per direction when both are
+// active, else each active cell's own element
+template <int S>
+__device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)[19], const bool (&act)[2], int ip0,
+                                               [[maybe_unused]] uint64_t pol)
+{
+    using T = typename Codec<S>::T;
     if (act[0] && act[1]) {
 #pragma unroll
-        for (int q = 0; q < 19; q++)
-            *reinterpret_cast<uint32_t*>(static_cast<T*>(a.fout_q[q]) + ip0) = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
+        for (int q = 0; q < 19; q++) {
+            T* p = static_cast<T*>(a.fout_q[q]) + ip0;
+            const uint32_t wd = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
+            if constexpr (LBFFS_BULK_EVICT) st_hint_b32(p, wd, pol);
+            else *reinterpret_cast<uint32_t*>(p) = wd;
+        }
     } else {
 #pragma unroll
         for (int q = 0; q < 19; q++) {
@@ -493,6 +572,24 @@ __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (
             if (act[1]) Codec<S>::store_held(p + 1, lane1(ft[q]));
         }
     }
+}
+
+__device__ __forceinline__ uint64_t bulk_policy(const StepArgs& a)
+{
+    if constexpr (LBFFS_BULK_EVICT) return a.l2_first ? l2_policy_evict_first() : l2_policy_evict_normal();
+    return 0;
+}
+
+template <int S, bool LES>
+__device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
+                                              const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
+                                              const int (&ic)[2], int ip0, bool plain = false)
+{
+    const uint64_t pol = bulk_policy(a);
+    F2 ft[19];
+    pair_adj_load<S>(a, ip0, act[0] || act[1], pol, ft);
+    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+    pair_adj_store<S>(a, ft, act, ip0, pol);
 }
 
 // One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
@@ -1022,6 +1119,8 @@ __device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)
     const bool face = (bw >> 9) & 1;
     const int N[3] = {g.nx, g.ny, g.nz};
     const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
+    [[maybe_unused]] uint64_t pol = 0;
+    if constexpr (LBFFS_HALO_KEEP) pol = l2_policy_evict_last();
     W v[NQ];
 #pragma unroll
     for (int n = 0; n < NQ; n++) {
@@ -1042,7 +1141,10 @@ __device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)
         }
         const int src_q = miss ? halo_missing<Q>(dq, bcode) : q;
         const int src_i = miss ? ip : g.porg + up[2] * g.pxy + up[1] * g.px + up[0];
-        v[n] = __ldg(f + (long long)src_q * g.pE + src_i);
+        const W* src = f + (long long)src_q * g.pE + src_i;
+        if constexpr (!LBFFS_HALO_KEEP) v[n] = __ldg(src);
+        else if constexpr (sizeof(W) == 2) v[n] = ld_hint_b16(src, pol);
+        else v[n] = ld_hint_b32(src, pol);
     }
     // an x ghost sits alone in the padding sector before / after its row: writing the whole
     // 32-byte sector avoids a read-modify-write of a partly written sector
@@ -1057,8 +1159,16 @@ __device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)
             W* sec = f + (HI ? dst : dst - (A - 1));
             const uint32_t w32 = sizeof(W) == 4 ? (uint32_t)v[n] : ((uint32_t)v[n] | ((uint32_t)v[n] << 16));
             const uint4 quad = make_uint4(w32, w32, w32, w32);
-            reinterpret_cast<uint4*>(sec)[0] = quad;
-            reinterpret_cast<uint4*>(sec)[1] = quad;
+            if constexpr (LBFFS_HALO_KEEP) {
+                st_hint_v4(sec, quad, pol);
+                st_hint_v4(reinterpret_cast<uint4*>(sec) + 1, quad, pol);
+            } else {
+                reinterpret_cast<uint4*>(sec)[0] = quad;
+                reinterpret_cast<uint4*>(sec)[1] = quad;
+            }
+        } else if constexpr (LBFFS_HALO_KEEP) {
+            if constexpr (sizeof(W) == 2) st_hint_b16(f + dst, v[n], pol);
+            else st_hint_b32(f + dst, v[n], pol);
         } else {
             f[dst] = v[n];
         }
