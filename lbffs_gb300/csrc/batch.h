@@ -10,6 +10,7 @@ namespace lbffs {
 
 struct BatchCase {
     StepArgs args[2];  // args[p]: source populations and macroscopics are copy p
+    StepArgs last;     // the final step's arguments (args[(nsteps - 1) & 1], full macroscopic fields)
     long long nsteps;  // steps the case runs in total
     int slot;          // index of the case's step counter
     int seg_per_row;   // 32-cell x segments per row: ceil(nx / 32)

@@ -39,11 +39,18 @@ __device__ __forceinline__ int find_case(const T* __restrict__ start, int n, T k
 #define LBFFS_BATCH_BOUNDS __launch_bounds__(BULK_BX)
 #endif
 
+// kernel arguments of the batched bulk kernel: 1 = a copy in shared memory per CTA, 0 = read
+// in place from the case table (cached); a build-time choice
+#ifndef LBFFS_BATCH_ARGS_SMEM
+#define LBFFS_BATCH_ARGS_SMEM 0
+#endif
+
 template <bool LES>
 __global__ void LBFFS_BATCH_BOUNDS k_bulk_batch(const BatchCase* __restrict__ cases,
                                                         const int* __restrict__ tile_start, int ncases,
                                                         const long long* __restrict__ done)
 {
+#if LBFFS_BATCH_ARGS_SMEM
     __shared__ StepArgs sa;
     __shared__ int s_case, s_parity, s_last;
     if (threadIdx.x == 0) {
@@ -61,8 +68,16 @@ __global__ void LBFFS_BATCH_BOUNDS k_bulk_batch(const BatchCase* __restrict__ ca
     __syncthreads();
     if (threadIdx.x == 0 && s_last) sa.store_all = 1;  // full macroscopic fields on the final step
     __syncthreads();
-    const int run = (int)blockIdx.x - tile_start[s_case];
-    const int spr = cases[s_case].seg_per_row, tiles = cases[s_case].tiles;
+    const int c = s_case;
+#else
+    // every thread finds the case (the same few cached words): no barrier before the work
+    const int c = find_case<int>(tile_start, ncases, (int)blockIdx.x);
+    const long long d = done[cases[c].slot];
+    if (d >= cases[c].nsteps) return;  // the case has finished; it leaves the batch at the next rebuild
+    const StepArgs& sa = d + 1 == cases[c].nsteps ? cases[c].last : cases[c].args[d & 1];
+#endif
+    const int run = (int)blockIdx.x - tile_start[c];
+    const int spr = cases[c].seg_per_row, tiles = cases[c].tiles;
     const int nseg = spr * sa.ny * sa.nz;
     const int t1 = min(tiles, (run + 1) * BATCH_TILES_PER_CTA);
     for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++)

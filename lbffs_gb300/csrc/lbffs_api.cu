@@ -575,7 +575,7 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
     a.tau_n = mn[4];
     a.store_all = p->store_fields == 2;
     a.bulk_kind = c->Q == 19 ? c->bulk_kind : 0;
-    a.l2_first = 2LL * c->Q * c->pg.pE * c->tsize <= c->l2_bytes;
+    a.l2_policy = 2LL * c->Q * c->pg.pE * c->tsize <= c->l2_bytes ? 1 : 0;
 }
 
 extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)

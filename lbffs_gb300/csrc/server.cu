@@ -283,11 +283,12 @@ cudaError_t build_batch(lbffs_server* s)
             lbffs_ctx* c = r->ctx;
             for (int p = 0; p < 2; p++) {
                 ctx_step_args(c, &r->params, p, p, hc[i].args[p]);
-                // the resident cases together exceed L2, whatever one case's size: streamed
-                // populations keep the normal eviction priority (evict-first measured 3 % slower
-                // on the served sample)
-                hc[i].args[p].l2_first = 0;
+                // the resident cases together exceed L2, whatever one case's size: no policy
+                // (evict-first measured 3 % slower on the served sample)
+                hc[i].args[p].l2_policy = 0;
             }
+            hc[i].last = hc[i].args[(r->nsteps - 1) & 1];
+            hc[i].last.store_all = 1;
             hc[i].nsteps = r->nsteps;
             hc[i].slot = r->slot;
             hc[i].seg_per_row = (c->d.nx + 31) / 32;

@@ -34,11 +34,12 @@ constexpr int SPECIAL_BS = 128;
 #define LBFFS_BULK_ADJ 1
 #endif
 // L2 eviction priority of the 2-byte bulk pair path's pulls and stores: with LBFFS_BULK_EVICT 1
-// they carry an L2 policy, evict-first when both population copies fit in L2 (StepArgs::l2_first:
-// the boundary kernel's scattered accesses then stay cached; 1024x256x4 FP16S cylinder channel
-// +22 % MLUPS) and evict-normal otherwise (on a 256^3 lattice evict-first measured 11 % slower:
-// adjacent warps' shared sectors were evicted before their second read).  The ghost fill's
-// accesses with LBFFS_HALO_KEEP 1 are evict-last (measured no better).  Build-time choices.
+// they carry the L2 policy StepArgs::l2_policy chooses: evict-first when both population copies
+// fit in L2 (the boundary kernel's scattered accesses then stay cached; 1024x256x4 FP16S cylinder
+// channel +22 % MLUPS), none otherwise (256^3: evict-first measured 11 % slower, adjacent warps'
+// shared sectors being evicted before their second read; evict-normal the same as none) and for
+// the server's batches.  The ghost fill's accesses with LBFFS_HALO_KEEP 1 are evict-last
+// (measured no better).  Build-time choices.
 #ifndef LBFFS_BULK_EVICT
 #define LBFFS_BULK_EVICT 1
 #endif
@@ -521,7 +522,7 @@ __device__ __forceinline__ float held_bits(__nv_bfloat16, uint16_t b) { return _
 // even), and when both cells are active their results leave as one packed 32-bit store.  Both
 // cells' pulls are read when either is active (the row is padded by a ghost cell on each side).
 // the 19 pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol
-template <int S>
+template <int S, bool HINT>
 __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool any, [[maybe_unused]] uint64_t pol,
                                               F2 (&ft)[19])
 {
@@ -532,12 +533,12 @@ __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool a
         const T* p = static_cast<const T*>(a.fin_s[q]) + ip0;
         if (lat_c(19, q, 0) == 0) {
             uint32_t wd = 0u;
-            if constexpr (LBFFS_BULK_EVICT) wd = any ? ld_hint_b32(p, pol) : 0u;
+            if constexpr (HINT) wd = any ? ld_hint_b32(p, pol) : 0u;
             else wd = any ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
             ft[q] = held_unpack(T{}, wd);
         } else {
             float x0, x1;
-            if constexpr (LBFFS_BULK_EVICT) {
+            if constexpr (HINT) {
                 x0 = any ? held_bits(T{}, ld_hint_b16(p, pol)) : 0.f;
                 x1 = any ? held_bits(T{}, ld_hint_b16(p + 1, pol)) : 0.f;
             } else {
@@ -551,7 +552,7 @@ __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool a
 
 // the results of two adjacent cells at ip0: one packed 32-bit store per direction when both are
 // active, else each active cell's own element
-template <int S>
+template <int S, bool HINT>
 __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)[19], const bool (&act)[2], int ip0,
                                                [[maybe_unused]] uint64_t pol)
 {
@@ -561,7 +562,7 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
         for (int q = 0; q < 19; q++) {
             T* p = static_cast<T*>(a.fout_q[q]) + ip0;
             const uint32_t wd = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
-            if constexpr (LBFFS_BULK_EVICT) st_hint_b32(p, wd, pol);
+            if constexpr (HINT) st_hint_b32(p, wd, pol);
             else *reinterpret_cast<uint32_t*>(p) = wd;
         }
     } else {
@@ -574,22 +575,22 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
     }
 }
 
-__device__ __forceinline__ uint64_t bulk_policy(const StepArgs& a)
-{
-    if constexpr (LBFFS_BULK_EVICT) return a.l2_first ? l2_policy_evict_first() : l2_policy_evict_normal();
-    return 0;
-}
-
 template <int S, bool LES>
 __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                               const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
                                               const int (&ic)[2], int ip0, bool plain = false)
 {
-    const uint64_t pol = bulk_policy(a);
     F2 ft[19];
-    pair_adj_load<S>(a, ip0, act[0] || act[1], pol, ft);
-    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
-    pair_adj_store<S>(a, ft, act, ip0, pol);
+    if (LBFFS_BULK_EVICT && a.l2_policy != 0) {
+        const uint64_t pol = a.l2_policy == 1 ? l2_policy_evict_first() : l2_policy_evict_normal();
+        pair_adj_load<S, true>(a, ip0, act[0] || act[1], pol, ft);
+        bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+        pair_adj_store<S, true>(a, ft, act, ip0, pol);
+    } else {
+        pair_adj_load<S, false>(a, ip0, act[0] || act[1], 0, ft);
+        bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+        pair_adj_store<S, false>(a, ft, act, ip0, 0);
+    }
 }
 
 // One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
@@ -931,36 +932,70 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     if (a.nei_solid[ic] == 1) {
         const float rho_o = a.rho_p[ic], tau_o = a.tau_p[ic];
         const float usq = uo[0] * uo[0] + uo[1] * uo[1] + uo[2] * uo[2];
+        // The loads run in phases, each phase's loads of all directions in flight together (a
+        // link's values depend on whether it is a link, and the IBB neighbour on the wall
+        // distance): which directions are links, then their bounce-back populations and wall
+        // distances, then the fluid-side velocities; the arithmetic below is unchanged.
+        long long upq[Q];
+        uint8_t sol[Q];
 #pragma unroll
         for (int q = 1; q < Q; q++) {
-            const long long up = upwind<Q>(q, x, N, b, face);
-            if (up < 0 || a.solid[up] != 1) continue;
-            const int qb = lat_opp(Q, q);
-            const float fb = F(qb, ip);
-            if (a.wall == WALL_BB) {
-                ft[q] = fb;
-            } else {
-                const float sdf0 = a.sdf[ic], sdf1 = a.sdf[up];
-                const float qf = fabsf(sdf0) / (fabsf(sdf0) + fabsf(sdf1));
-                const float we = 1.f / (1.f / omega + tau_o);
-                const float uc = -uo[0] * (float)lat_c(Q, q, 0) - uo[1] * (float)lat_c(Q, q, 1) - uo[2] * (float)lat_c(Q, q, 2);
-                float feq, chi;
-                if (qf <= 0.5f) {
-                    const long long fl = upwind<Q>(qb, x, N, b, face);
-                    const long long fc = fl < 0 ? ic : fl;
-                    const float ufc = -a.u_p[fc] * (float)lat_c(Q, q, 0) - a.v_p[fc] * (float)lat_c(Q, q, 1) -
-                                      a.w_p[fc] * (float)lat_c(Q, q, 2);
-                    feq = (rho_o + 3.f * ufc + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
-                    chi = we * (2.f * qf - 1.f) / (1.f - 2.f * we);
-                } else {
-                    feq = (rho_o + 3.f * (1.f - 1.f / qf) * uc + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
-                    chi = we * (2.f * qf - 1.f);
+            upq[q] = upwind<Q>(q, x, N, b, face);
+            sol[q] = upq[q] >= 0 ? a.solid[upq[q]] : (uint8_t)0;
+        }
+        unsigned links = 0;
+#pragma unroll
+        for (int q = 1; q < Q; q++)
+            if (upq[q] >= 0 && sol[q] == 1) links |= 1u << q;
+        if (links) {
+            const bool ibb = a.wall != WALL_BB;
+            const float sdf0 = ibb ? a.sdf[ic] : 0.f;
+            float fbq[Q], qfq[Q], ufq[Q];
+#pragma unroll
+            for (int q = 1; q < Q; q++) {
+                fbq[q] = 0.f;
+                qfq[q] = 1.f;
+                if (!((links >> q) & 1u)) continue;
+                fbq[q] = F(lat_opp(Q, q), ip);
+                if (ibb) {
+                    const float sdf1 = a.sdf[upq[q]];
+                    qfq[q] = fabsf(sdf0) / (fabsf(sdf0) + fabsf(sdf1));
                 }
-                ft[q] = (1.f - chi) * fb + chi * feq;
             }
 #pragma unroll
-            for (int d = 0; d < 3; d++)
-                if (lat_c(Q, q, d)) fw[d] += -(fb + ft[q]) * (float)lat_c(Q, q, d);
+            for (int q = 1; q < Q; q++) {
+                ufq[q] = 0.f;
+                if (!((links >> q) & 1u) || !ibb || !(qfq[q] <= 0.5f)) continue;
+                const long long fl = upwind<Q>(lat_opp(Q, q), x, N, b, face);
+                const long long fc = fl < 0 ? ic : fl;
+                ufq[q] = -a.u_p[fc] * (float)lat_c(Q, q, 0) - a.v_p[fc] * (float)lat_c(Q, q, 1) -
+                         a.w_p[fc] * (float)lat_c(Q, q, 2);
+            }
+#pragma unroll
+            for (int q = 1; q < Q; q++) {
+                if (!((links >> q) & 1u)) continue;
+                const float fb = fbq[q];
+                if (!ibb) {
+                    ft[q] = fb;
+                } else {
+                    const float qf = qfq[q];
+                    const float we = 1.f / (1.f / omega + tau_o);
+                    const float uc =
+                        -uo[0] * (float)lat_c(Q, q, 0) - uo[1] * (float)lat_c(Q, q, 1) - uo[2] * (float)lat_c(Q, q, 2);
+                    float feq, chi;
+                    if (qf <= 0.5f) {
+                        feq = (rho_o + 3.f * ufq[q] + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
+                        chi = we * (2.f * qf - 1.f) / (1.f - 2.f * we);
+                    } else {
+                        feq = (rho_o + 3.f * (1.f - 1.f / qf) * uc + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
+                        chi = we * (2.f * qf - 1.f);
+                    }
+                    ft[q] = (1.f - chi) * fb + chi * feq;
+                }
+#pragma unroll
+                for (int d = 0; d < 3; d++)
+                    if (lat_c(Q, q, d)) fw[d] += -(fb + ft[q]) * (float)lat_c(Q, q, d);
+            }
         }
     }
     a.fwx[ic] = fw[0];
