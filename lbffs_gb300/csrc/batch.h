@@ -15,6 +15,7 @@ struct BatchCase {
     int slot;          // index of the case's step counter
     int seg_per_row;   // 32-cell x segments per row: ceil(nx / 32)
     int tiles;         // bulk tiles of the case: ceil(seg_per_row * ny * nz / BATCH_SEG_PER_TILE)
+    FastDiv dspr, dny;  // division by seg_per_row and by ny
 };
 
 // x segments one bulk tile covers (BULK_V per warp of a BULK_BX-thread CTA; bulk_segments)

@@ -81,7 +81,8 @@ __global__ void LBFFS_BATCH_BOUNDS k_bulk_batch(const BatchCase* __restrict__ ca
     const int nseg = spr * sa.ny * sa.nz;
     const int t1 = min(tiles, (run + 1) * BATCH_TILES_PER_CTA);
     for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++)
-        bulk_segments<19, S, COLL_RR, SGS_SMAG, LES>(sa, tile * BATCH_SEG_PER_TILE, spr, nseg);
+        bulk_segments<19, S, COLL_RR, SGS_SMAG, LES>(sa, tile * BATCH_SEG_PER_TILE, spr, nseg, cases[c].dspr,
+                                                     cases[c].dny);
 }
 
 __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* __restrict__ cases,

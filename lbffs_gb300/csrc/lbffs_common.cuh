@@ -150,6 +150,26 @@ struct Codec<ST_BF16S> {
     static __device__ __forceinline__ void store_held(T* p, float g) { *p = __float2bfloat16_rn(g); }
 };
 
+// x / d for 0 <= x < 2^31 by a multiply-high and a shift (round-up method of Granlund and
+// Montgomery, 1994): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, x / d = (mulhi(x, m) + x)
+// >> l, the sum staying below 2^32 for x < 2^31
+struct FastDiv {
+    uint32_t m;
+    int l;
+};
+inline FastDiv fast_div(uint32_t d)
+{
+    int l = 0;
+    while ((1ull << l) < d) l++;
+    const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{(uint32_t)m, l};
+}
+__device__ __forceinline__ int fdiv(int x, FastDiv f)
+{
+    const uint32_t t = __umulhi((uint32_t)x, f.m);
+    return (int)((t + (uint32_t)x) >> f.l);
+}
+
 // Padded population planes: cell (i,j,k) at porg + k*pxy + j*px + i of a plane of pE elements.
 struct PadGeom {
     int nx, ny, nz, px, pxy, porg;

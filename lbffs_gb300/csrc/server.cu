@@ -292,6 +292,8 @@ cudaError_t build_batch(lbffs_server* s)
             hc[i].nsteps = r->nsteps;
             hc[i].slot = r->slot;
             hc[i].seg_per_row = (c->d.nx + 31) / 32;
+            hc[i].dspr = fast_div((uint32_t)hc[i].seg_per_row);
+            hc[i].dny = fast_div((uint32_t)c->d.ny);
             hc[i].tiles = (int)(((long long)hc[i].seg_per_row * c->d.ny * c->d.nz + BATCH_SEG_PER_TILE - 1) /
                                 BATCH_SEG_PER_TILE);
             tiles[i + 1] = tiles[i] + (hc[i].tiles + BATCH_TILES_PER_CTA - 1) / BATCH_TILES_PER_CTA;

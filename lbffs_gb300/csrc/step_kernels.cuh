@@ -517,10 +517,6 @@ __device__ __forceinline__ void st_hint_v4(void* p, uint4 v, uint64_t pol)
 __device__ __forceinline__ float held_bits(__half, uint16_t b) { return __half2float(__ushort_as_half(b)); }
 __device__ __forceinline__ float held_bits(__nv_bfloat16, uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
 
-// bulk_pair for two adjacent cells of 2-byte storage (ip0 even, cell ip0 + 1 the second): the
-// pulls with c_x = 0 of both cells are one aligned 32-bit word (the pull offset c_y px + c_z pxy is
-// even), and when both cells are active their results leave as one packed 32-bit store.  Both
-// cells' pulls are read when either is active (the row is padded by a ghost cell on each side).
 // the 19 pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol
 template <int S, bool HINT>
 __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool any, [[maybe_unused]] uint64_t pol,
@@ -575,6 +571,10 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
     }
 }
 
+// bulk_pair for two adjacent cells of 2-byte storage (ip0 even, cell ip0 + 1 the second): the
+// pulls with c_x = 0 of both cells are one aligned 32-bit word (the pull offset c_y px + c_z pxy is
+// even), and when both cells are active their results leave as one packed 32-bit store.  Both
+// cells' pulls are read when either is active (the row is padded by a ghost cell on each side).
 template <int S, bool LES>
 __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                               const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
@@ -680,9 +680,10 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
 // Segment mapping of the same per-cell work, for lattices with narrow rows: a row is cut into
 // ceil(nx / 32) segments of 32 cells, segments are numbered row after row ((j, k) order), and warp
 // w of the CTA takes segments g0 + BULK_V * w + v.  A 24-cell row then keeps 24 of 32 lanes busy
-// where a BULK_BX * BULK_V-cell row tile keeps 24 of 256.  spr = segments per row, nseg = all.
+// where a BULK_BX * BULK_V-cell row tile keeps 24 of 256.  spr = segments per row, nseg = all;
+// dspr / dny divide by spr and ny.
 template <int Q, int S, int COLL, int SGS, bool LES>
-__device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr, int nseg)
+__device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr, int nseg, FastDiv dspr, FastDiv dny)
 {
     using T = typename Codec<S>::T;
     constexpr bool HELD = (Q == 19);
@@ -697,10 +698,10 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
 #pragma unroll
     for (int v = 0; v < BULK_V; v++) {
         const int g = ADJ ? g0 + warp * BULK_V + (lane >> 4) : g0 + warp * BULK_V + v;
-        const int row = g / spr;
+        const int row = fdiv(g, dspr);
         ci[v] = ADJ ? (g - row * spr) * 32 + 2 * (lane & 15) + v : (g - row * spr) * 32 + lane;
-        cj[v] = row % a.ny;
-        ck[v] = row / a.ny;
+        ck[v] = fdiv(row, dny);
+        cj[v] = row - ck[v] * a.ny;
         fl[v] = (g < nseg && ci[v] < a.nx) ? __ldg(a.flags + (long long)row * a.nx + ci[v]) : FL_SOLID;
         act[v] = !(fl[v] & (FL_SOLID | FL_SPECIAL));
         any |= act[v];
@@ -932,70 +933,36 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     if (a.nei_solid[ic] == 1) {
         const float rho_o = a.rho_p[ic], tau_o = a.tau_p[ic];
         const float usq = uo[0] * uo[0] + uo[1] * uo[1] + uo[2] * uo[2];
-        // The loads run in phases, each phase's loads of all directions in flight together (a
-        // link's values depend on whether it is a link, and the IBB neighbour on the wall
-        // distance): which directions are links, then their bounce-back populations and wall
-        // distances, then the fluid-side velocities; the arithmetic below is unchanged.
-        long long upq[Q];
-        uint8_t sol[Q];
 #pragma unroll
         for (int q = 1; q < Q; q++) {
-            upq[q] = upwind<Q>(q, x, N, b, face);
-            sol[q] = upq[q] >= 0 ? a.solid[upq[q]] : (uint8_t)0;
-        }
-        unsigned links = 0;
-#pragma unroll
-        for (int q = 1; q < Q; q++)
-            if (upq[q] >= 0 && sol[q] == 1) links |= 1u << q;
-        if (links) {
-            const bool ibb = a.wall != WALL_BB;
-            const float sdf0 = ibb ? a.sdf[ic] : 0.f;
-            float fbq[Q], qfq[Q], ufq[Q];
-#pragma unroll
-            for (int q = 1; q < Q; q++) {
-                fbq[q] = 0.f;
-                qfq[q] = 1.f;
-                if (!((links >> q) & 1u)) continue;
-                fbq[q] = F(lat_opp(Q, q), ip);
-                if (ibb) {
-                    const float sdf1 = a.sdf[upq[q]];
-                    qfq[q] = fabsf(sdf0) / (fabsf(sdf0) + fabsf(sdf1));
-                }
-            }
-#pragma unroll
-            for (int q = 1; q < Q; q++) {
-                ufq[q] = 0.f;
-                if (!((links >> q) & 1u) || !ibb || !(qfq[q] <= 0.5f)) continue;
-                const long long fl = upwind<Q>(lat_opp(Q, q), x, N, b, face);
-                const long long fc = fl < 0 ? ic : fl;
-                ufq[q] = -a.u_p[fc] * (float)lat_c(Q, q, 0) - a.v_p[fc] * (float)lat_c(Q, q, 1) -
-                         a.w_p[fc] * (float)lat_c(Q, q, 2);
-            }
-#pragma unroll
-            for (int q = 1; q < Q; q++) {
-                if (!((links >> q) & 1u)) continue;
-                const float fb = fbq[q];
-                if (!ibb) {
-                    ft[q] = fb;
+            const long long up = upwind<Q>(q, x, N, b, face);
+            if (up < 0 || a.solid[up] != 1) continue;
+            const int qb = lat_opp(Q, q);
+            const float fb = F(qb, ip);
+            if (a.wall == WALL_BB) {
+                ft[q] = fb;
+            } else {
+                const float sdf0 = a.sdf[ic], sdf1 = a.sdf[up];
+                const float qf = fabsf(sdf0) / (fabsf(sdf0) + fabsf(sdf1));
+                const float we = 1.f / (1.f / omega + tau_o);
+                const float uc = -uo[0] * (float)lat_c(Q, q, 0) - uo[1] * (float)lat_c(Q, q, 1) - uo[2] * (float)lat_c(Q, q, 2);
+                float feq, chi;
+                if (qf <= 0.5f) {
+                    const long long fl = upwind<Q>(qb, x, N, b, face);
+                    const long long fc = fl < 0 ? ic : fl;
+                    const float ufc = -a.u_p[fc] * (float)lat_c(Q, q, 0) - a.v_p[fc] * (float)lat_c(Q, q, 1) -
+                                      a.w_p[fc] * (float)lat_c(Q, q, 2);
+                    feq = (rho_o + 3.f * ufc + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
+                    chi = we * (2.f * qf - 1.f) / (1.f - 2.f * we);
                 } else {
-                    const float qf = qfq[q];
-                    const float we = 1.f / (1.f / omega + tau_o);
-                    const float uc =
-                        -uo[0] * (float)lat_c(Q, q, 0) - uo[1] * (float)lat_c(Q, q, 1) - uo[2] * (float)lat_c(Q, q, 2);
-                    float feq, chi;
-                    if (qf <= 0.5f) {
-                        feq = (rho_o + 3.f * ufq[q] + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
-                        chi = we * (2.f * qf - 1.f) / (1.f - 2.f * we);
-                    } else {
-                        feq = (rho_o + 3.f * (1.f - 1.f / qf) * uc + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
-                        chi = we * (2.f * qf - 1.f);
-                    }
-                    ft[q] = (1.f - chi) * fb + chi * feq;
+                    feq = (rho_o + 3.f * (1.f - 1.f / qf) * uc + 4.5f * uc * uc - 1.5f * usq) * lat_w(Q, q);
+                    chi = we * (2.f * qf - 1.f);
                 }
-#pragma unroll
-                for (int d = 0; d < 3; d++)
-                    if (lat_c(Q, q, d)) fw[d] += -(fb + ft[q]) * (float)lat_c(Q, q, d);
+                ft[q] = (1.f - chi) * fb + chi * feq;
             }
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+                if (lat_c(Q, q, d)) fw[d] += -(fb + ft[q]) * (float)lat_c(Q, q, d);
         }
     }
     a.fwx[ic] = fw[0];
