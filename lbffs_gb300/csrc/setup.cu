@@ -5,6 +5,7 @@
 // geometry change into a u16 boundary word and a u8 flag per cell plus a compact list
 // of the cells that need the general boundary path; the time step never touches the
 // int32 arrays again.
+#include <algorithm>
 #include <climits>
 
 #include "launch.h"
@@ -285,23 +286,35 @@ cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long 
 }
 
 // ---- ghost layer (halo_block in step_kernels.cuh) ----
-template <int Q, typename W>
+template <int Q, typename W, bool SPEC>
 __global__ void __launch_bounds__(HALO_BS) k_halo(W* f, const uint8_t* __restrict__ flags,
                                                   const uint16_t* __restrict__ bc, PadGeom g)
 {
-    halo_block<Q, W>(f, flags, bc, g, blockIdx.x, threadIdx.x);
+    halo_block<Q, W, SPEC>(f, flags, bc, g, blockIdx.x, threadIdx.x);
+}
+
+template <int Q, typename W>
+static void launch_halo(bool spec, long long nb, void* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
+                        cudaStream_t st)
+{
+    if (spec) k_halo<Q, W, true><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<W*>(f), flags, bc, g);
+    else k_halo<Q, W, false><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<W*>(f), flags, bc, g);
 }
 
 cudaError_t halo_fill(int Q, int tsize, void* f, const uint8_t* flags, const uint16_t* bc, const PadGeom& g,
                       cudaStream_t st)
 {
-    const long long nb = halo_blocks(g, Q, 0) + halo_blocks(g, Q, 1) + halo_blocks(g, Q, 2);
+    const long long n0 = halo_blocks(g, Q, 0), n1 = halo_blocks(g, Q, 1), n2 = halo_blocks(g, Q, 2);
+    const long long nb = n0 + n1 + n2;
+    // D3Q19: the per-face code paths when one axis holds at least two thirds of the face cells
+    // (the run-time path is measured on D3Q19 only; D3Q27 keeps the per-face paths)
+    const bool spec = Q != 19 || 3 * std::max(n0, std::max(n1, n2)) >= 2 * nb;
     if (Q == 19) {
-        if (tsize == 4) k_halo<19, uint32_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g);
-        else k_halo<19, uint16_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g);
+        if (tsize == 4) launch_halo<19, uint32_t>(spec, nb, f, flags, bc, g, st);
+        else launch_halo<19, uint16_t>(spec, nb, f, flags, bc, g, st);
     } else {
-        if (tsize == 4) k_halo<27, uint32_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint32_t*>(f), flags, bc, g);
-        else k_halo<27, uint16_t><<<(unsigned)nb, HALO_BS, 0, st>>>(static_cast<uint16_t*>(f), flags, bc, g);
+        if (tsize == 4) launch_halo<27, uint32_t>(spec, nb, f, flags, bc, g, st);
+        else launch_halo<27, uint16_t>(spec, nb, f, flags, bc, g, st);
     }
     return cudaGetLastError();
 }

