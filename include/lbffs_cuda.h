@@ -181,8 +181,9 @@ int lbffs_cell_counts(lbffs_ctx* ctx, long long out[4]);
 
 /* No counterpart in the reference (a choice between two implementations of the same D3Q19 step,
    which give identical results).  kind 0: each thread loads its cells' pulled populations from
-   HBM; kind 1: the pulled rows of a tile are staged in shared memory by bulk async copies and
-   clean tiles are written back the same way.  D3Q27 contexts always use kind 0. */
+   HBM; kind 1: a producer warp per CTA streams the pulled rows of each 256-cell row tile into a
+   ring of shared-memory stages by bulk async copies and four consumer warps collide from there.
+   D3Q27 contexts always use kind 0. */
 int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
 
 /* setSolid + setNeiSolid (src/walls.hpp:159-216) on the device, bit for bit the reference's host

@@ -28,6 +28,11 @@ constexpr int SPECIAL_BS = 128;
 // CTAs ahead whose pulled rows a 2-byte D3Q19 bulk CTA prefetches into L2 (0: none); a build-time
 // tuning value.  608 (half a wave of 8-CTA-per-SM residency) measured 4 % faster on the 256^3
 // FP16S / BF16S cavity than none or 304, the same as 1216.
+// 2-byte D3Q19 bulk cells of k_bulk: the pulls are issued together with the flag loads (1) or
+// after them (0); a build-time choice
+#ifndef LBFFS_BULK_EAGER
+#define LBFFS_BULK_EAGER 1
+#endif
 // 2-byte D3Q19 bulk cells: a lane owns two adjacent cells (1) or two cells 32 apart (0); a
 // build-time choice
 #ifndef LBFFS_BULK_ADJ
@@ -593,6 +598,63 @@ __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (
     }
 }
 
+// 2-byte D3Q19 storage: L2 prefetch of the rows the CTA LBFFS_BULK_PREFETCH launches ahead will
+// pull (one bulk prefetch per direction, issued by the first Q threads; the range is shrunk to
+// whole 16-byte units inside the pulled elements, so it never leaves the population planes).  The
+// 2-byte kernel is latency-bound with half the bytes in flight of FP32; for the bandwidth-bound
+// FP32 and D3Q27 kernels the extra requests measured slower.
+template <int Q, int S, int V>
+__device__ __forceinline__ void bulk_prefetch(const StepArgs& a)
+{
+#if LBFFS_BULK_PREFETCH > 0
+    using T = typename Codec<S>::T;
+    if (Q == 19 && S != ST_FP32 && threadIdx.x < Q) {
+        const long long nb = (long long)gridDim.x * gridDim.y * gridDim.z;
+        const long long fb = (long long)blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z) +
+                             LBFFS_BULK_PREFETCH;
+        if (fb < nb) {
+            const int fx = (int)(fb % gridDim.x), fr = (int)(fb / gridDim.x);
+            const int fj = fr % a.ny, fk = fr / a.ny;
+            const int x0 = fx * BULK_BX * V, n = min(BULK_BX * V, a.nx - x0);
+            const uintptr_t base = reinterpret_cast<uintptr_t>(a.fin_s[threadIdx.x]);
+            const uintptr_t lo = base + (uintptr_t)pidx(a, x0, fj, fk) * sizeof(T);
+            const uintptr_t b0 = (lo + 15) & ~(uintptr_t)15, b1 = (lo + (uintptr_t)n * sizeof(T)) & ~(uintptr_t)15;
+            if (b1 > b0)
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b0), "r"((unsigned)(b1 - b0)) : "memory");
+        }
+    }
+#endif
+}
+
+// The adjacent pair of a bulk_block lane with its pulls issued together with its flag loads
+// (one memory round trip before the collision instead of two): the pair's pulls are read whenever
+// its first cell is in the row, active or not (a solid cell's values are read and dropped).
+template <int S, bool LES>
+__device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, int j, int k, int row, int prow)
+{
+    const bool valid = i0 < a.nx;
+    uint8_t fl[2];
+    fl[0] = valid ? __ldg(a.flags + row + i0) : FL_SOLID;
+    fl[1] = i0 + 1 < a.nx ? __ldg(a.flags + row + i0 + 1) : FL_SOLID;
+    const bool hint = LBFFS_BULK_EVICT && a.l2_policy != 0;
+    [[maybe_unused]] uint64_t pol = 0;
+    F2 ft[19];
+    if (hint) {
+        pol = a.l2_policy == 1 ? l2_policy_evict_first() : l2_policy_evict_normal();
+        pair_adj_load<S, true>(a, prow + i0, valid, pol, ft);
+    } else {
+        pair_adj_load<S, false>(a, prow + i0, valid, 0, ft);
+    }
+    const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
+    const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
+    if (!(act[0] || act[1])) return;
+    const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
+    const int ic[2] = {row + i0, row + i0 + 1};
+    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+    if (hint) pair_adj_store<S, true>(a, ft, act, prow + i0, pol);
+    else pair_adj_store<S, false>(a, ft, act, prow + i0, 0);
+}
+
 // One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
 // instruction of a warp covers 32 consecutive cells.  Every population is pulled from the same
 // offset for every cell: cells on the domain border read the ghost layer, which k_halo filled
@@ -613,6 +675,11 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     constexpr int DV = ADJ ? 1 : 32;  // x distance of a lane's consecutive cells
     const int row = (k * a.ny + j) * a.nx;
     const int prow = pidx(a, 0, j, k);
+    bulk_prefetch<Q, S, V>(a);
+    if constexpr (ADJ && LBFFS_BULK_EAGER) {
+        bulk_pair_adj_eager<S, LES>(a, i0, j, k, row, prow);
+        return;
+    }
     uint8_t fl[V];
     bool act[V];
     bool any = false;
@@ -626,28 +693,6 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     bool plain = false;
     if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
     if (!any) return;
-#if LBFFS_BULK_PREFETCH > 0
-    // 2-byte D3Q19 storage: L2 prefetch of the rows the CTA LBFFS_BULK_PREFETCH launches ahead
-    // will pull (one bulk prefetch per direction, issued by the first Q threads; the range is
-    // shrunk to whole 16-byte units inside the pulled elements, so it never leaves the population
-    // planes).  The 2-byte kernel is latency-bound with half the bytes in flight of FP32; for the
-    // bandwidth-bound FP32 and D3Q27 kernels the extra requests measured slower.
-    if (Q == 19 && S != ST_FP32 && threadIdx.x < Q) {
-        const long long nb = (long long)gridDim.x * gridDim.y * gridDim.z;
-        const long long fb = (long long)blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z) +
-                             LBFFS_BULK_PREFETCH;
-        if (fb < nb) {
-            const int fx = (int)(fb % gridDim.x), fr = (int)(fb / gridDim.x);
-            const int fj = fr % a.ny, fk = fr / a.ny;
-            const int x0 = fx * BULK_BX * V, n = min(BULK_BX * V, a.nx - x0);
-            const uintptr_t base = reinterpret_cast<uintptr_t>(a.fin_s[threadIdx.x]);
-            const uintptr_t lo = base + (uintptr_t)pidx(a, x0, fj, fk) * sizeof(T);
-            const uintptr_t b0 = (lo + 15) & ~(uintptr_t)15, b1 = (lo + (uintptr_t)n * sizeof(T)) & ~(uintptr_t)15;
-            if (b1 > b0)
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b0), "r"((unsigned)(b1 - b0)) : "memory");
-        }
-    }
-#endif
     if constexpr (ADJ) {
         const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 1};
