@@ -33,6 +33,15 @@ constexpr int SPECIAL_BS = 128;
 #ifndef LBFFS_BULK_EAGER
 #define LBFFS_BULK_EAGER 1
 #endif
+// packed 2-byte pair stores as streaming stores (st.global.cs, like the FP32 stores); a
+// build-time choice
+#ifndef LBFFS_BULK_STCS
+#define LBFFS_BULK_STCS 0
+#endif
+// the same for the D3Q19 pairs 32 apart (FP32 storage)
+#ifndef LBFFS_BULK_EAGER32
+#define LBFFS_BULK_EAGER32 1
+#endif
 // 2-byte D3Q19 bulk cells: a lane owns two adjacent cells (1) or two cells 32 apart (0); a
 // build-time choice
 #ifndef LBFFS_BULK_ADJ
@@ -564,6 +573,7 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
             T* p = static_cast<T*>(a.fout_q[q]) + ip0;
             const uint32_t wd = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
             if constexpr (HINT) st_hint_b32(p, wd, pol);
+            else if constexpr (LBFFS_BULK_STCS) __stcs(reinterpret_cast<unsigned int*>(p), wd);
             else *reinterpret_cast<uint32_t*>(p) = wd;
         }
     } else {
@@ -630,12 +640,13 @@ __device__ __forceinline__ void bulk_prefetch(const StepArgs& a)
 // (one memory round trip before the collision instead of two): the pair's pulls are read whenever
 // its first cell is in the row, active or not (a solid cell's values are read and dropped).
 template <int S, bool LES>
-__device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, int j, int k, int row, int prow)
+__device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, int j, int k, int row, int prow,
+                                                    bool inrange = true)
 {
-    const bool valid = i0 < a.nx;
+    const bool valid = inrange && i0 < a.nx;
     uint8_t fl[2];
     fl[0] = valid ? __ldg(a.flags + row + i0) : FL_SOLID;
-    fl[1] = i0 + 1 < a.nx ? __ldg(a.flags + row + i0 + 1) : FL_SOLID;
+    fl[1] = valid && i0 + 1 < a.nx ? __ldg(a.flags + row + i0 + 1) : FL_SOLID;
     const bool hint = LBFFS_BULK_EVICT && a.l2_policy != 0;
     [[maybe_unused]] uint64_t pol = 0;
     F2 ft[19];
@@ -653,6 +664,38 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
     bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
     if (hint) pair_adj_store<S, true>(a, ft, act, prow + i0, pol);
     else pair_adj_store<S, false>(a, ft, act, prow + i0, 0);
+}
+
+// bulk_pair (cells i0 and i0 + 32) with the pulls issued together with the flag loads; a cell's
+// pulls are read whenever it is in the row, active or not
+template <int S, bool LES>
+__device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j, int k, int row, int prow)
+{
+    using T = typename Codec<S>::T;
+    const bool valid[2] = {i0 < a.nx, i0 + 32 < a.nx};
+    uint8_t fl[2];
+    F2 ft[19];
+#pragma unroll
+    for (int v = 0; v < 2; v++) fl[v] = valid[v] ? __ldg(a.flags + row + i0 + 32 * v) : FL_SOLID;
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        const T* p = static_cast<const T*>(a.fin_s[q]) + prow + i0;
+        const float x0 = valid[0] ? Codec<S>::load_held(p) : 0.f;
+        const float x1 = valid[1] ? Codec<S>::load_held(p + 32) : 0.f;
+        ft[q] = pk(x0, x1);
+    }
+    const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
+    const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
+    if (!(act[0] || act[1])) return;
+    const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
+    const int ic[2] = {row + i0, row + i0 + 32};
+    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        T* p = static_cast<T*>(a.fout_q[q]) + prow + i0;
+        if (act[0]) Codec<S>::store_held(p, lane0(ft[q]));
+        if (act[1]) Codec<S>::store_held(p + 32, lane1(ft[q]));
+    }
 }
 
 // One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
@@ -678,6 +721,9 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     bulk_prefetch<Q, S, V>(a);
     if constexpr (ADJ && LBFFS_BULK_EAGER) {
         bulk_pair_adj_eager<S, LES>(a, i0, j, k, row, prow);
+        return;
+    } else if constexpr (Q == 19 && SGS != SGS_WALE && V == 2 && !ADJ && LBFFS_BULK_EAGER32) {
+        bulk_pair_eager<S, LES>(a, i0, j, k, row, prow);
         return;
     }
     uint8_t fl[V];
@@ -736,6 +782,15 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
     // lanes 16-31 of its second (bulk_pair_adj); otherwise lane l takes cell l of both segments
     constexpr bool ADJ = Q == 19 && SGS != SGS_WALE && BULK_V == 2 && S != ST_FP32 && LBFFS_BULK_ADJ;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if constexpr (ADJ && LBFFS_BULK_EAGER) {
+        const int g = g0 + warp * BULK_V + (lane >> 4);
+        const bool inrange = g < nseg;
+        const int row = inrange ? fdiv(g, dspr) : 0;
+        const int i0 = (g - row * spr) * 32 + 2 * (lane & 15);
+        const int k = fdiv(row, dny), j = row - k * a.ny;
+        bulk_pair_adj_eager<S, LES>(a, inrange ? i0 : a.nx, j, k, row * a.nx, pidx(a, 0, j, k), inrange);
+        return;
+    }
     int ci[BULK_V], cj[BULK_V], ck[BULK_V];
     uint8_t fl[BULK_V];
     bool act[BULK_V];
