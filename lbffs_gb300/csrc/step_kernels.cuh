@@ -33,11 +33,6 @@ constexpr int SPECIAL_BS = 128;
 #ifndef LBFFS_BULK_EAGER
 #define LBFFS_BULK_EAGER 1
 #endif
-// packed 2-byte pair stores as streaming stores (st.global.cs, like the FP32 stores); a
-// build-time choice
-#ifndef LBFFS_BULK_STCS
-#define LBFFS_BULK_STCS 0
-#endif
 // the same for the D3Q19 pairs 32 apart (FP32 storage)
 #ifndef LBFFS_BULK_EAGER32
 #define LBFFS_BULK_EAGER32 1
@@ -52,13 +47,10 @@ constexpr int SPECIAL_BS = 128;
 // fit in L2 (the boundary kernel's scattered accesses then stay cached; 1024x256x4 FP16S cylinder
 // channel +22 % MLUPS), none otherwise (256^3: evict-first measured 11 % slower, adjacent warps'
 // shared sectors being evicted before their second read; evict-normal the same as none) and for
-// the server's batches.  The ghost fill's accesses with LBFFS_HALO_KEEP 1 are evict-last
-// (measured no better).  Build-time choices.
+// the server's batches (an evict-last policy on the ghost fill's accesses measured no better).
+// A build-time choice.
 #ifndef LBFFS_BULK_EVICT
 #define LBFFS_BULK_EVICT 1
-#endif
-#ifndef LBFFS_HALO_KEEP
-#define LBFFS_HALO_KEEP 0
 #endif
 #ifndef LBFFS_BULK_PREFETCH
 #define LBFFS_BULK_PREFETCH 608
@@ -495,12 +487,6 @@ __device__ __forceinline__ uint64_t l2_policy_evict_normal()
     asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
     return p;
 }
-__device__ __forceinline__ uint64_t l2_policy_evict_last()
-{
-    uint64_t p;
-    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
 __device__ __forceinline__ uint32_t ld_hint_b32(const void* p, uint64_t pol)
 {
     uint32_t v;
@@ -516,16 +502,6 @@ __device__ __forceinline__ uint16_t ld_hint_b16(const void* p, uint64_t pol)
 __device__ __forceinline__ void st_hint_b32(void* p, uint32_t v, uint64_t pol)
 {
     asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
-}
-__device__ __forceinline__ void st_hint_b16(void* p, uint16_t v, uint64_t pol)
-{
-    asm volatile("st.global.L2::cache_hint.b16 [%0], %1, %2;" ::"l"(p), "h"(v), "l"(pol) : "memory");
-}
-__device__ __forceinline__ void st_hint_v4(void* p, uint4 v, uint64_t pol)
-{
-    asm volatile("st.global.L2::cache_hint.v4.b32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
-                 "r"(v.w), "l"(pol)
-                 : "memory");
 }
 // a stored 2-byte element (its bits) as the held value
 __device__ __forceinline__ float held_bits(__half, uint16_t b) { return __half2float(__ushort_as_half(b)); }
@@ -573,7 +549,6 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
             T* p = static_cast<T*>(a.fout_q[q]) + ip0;
             const uint32_t wd = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
             if constexpr (HINT) st_hint_b32(p, wd, pol);
-            else if constexpr (LBFFS_BULK_STCS) __stcs(reinterpret_cast<unsigned int*>(p), wd);
             else *reinterpret_cast<uint32_t*>(p) = wd;
         }
     } else {
@@ -1221,8 +1196,6 @@ __device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)
     const bool face = (bw >> 9) & 1;
     const int N[3] = {g.nx, g.ny, g.nz};
     const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
-    [[maybe_unused]] uint64_t pol = 0;
-    if constexpr (LBFFS_HALO_KEEP) pol = l2_policy_evict_last();
     W v[NQ];
 #pragma unroll
     for (int n = 0; n < NQ; n++) {
@@ -1243,10 +1216,7 @@ __device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)
         }
         const int src_q = miss ? halo_missing<Q>(dq, bcode) : q;
         const int src_i = miss ? ip : g.porg + up[2] * g.pxy + up[1] * g.px + up[0];
-        const W* src = f + (long long)src_q * g.pE + src_i;
-        if constexpr (!LBFFS_HALO_KEEP) v[n] = __ldg(src);
-        else if constexpr (sizeof(W) == 2) v[n] = ld_hint_b16(src, pol);
-        else v[n] = ld_hint_b32(src, pol);
+        v[n] = __ldg(f + (long long)src_q * g.pE + src_i);
     }
     // an x ghost sits alone in the padding sector before / after its row: writing the whole
     // 32-byte sector avoids a read-modify-write of a partly written sector
@@ -1261,16 +1231,8 @@ __device__ __forceinline__ void halo_cell(W* f, const PadGeom& g, const int (&x)
             W* sec = f + (HI ? dst : dst - (A - 1));
             const uint32_t w32 = sizeof(W) == 4 ? (uint32_t)v[n] : ((uint32_t)v[n] | ((uint32_t)v[n] << 16));
             const uint4 quad = make_uint4(w32, w32, w32, w32);
-            if constexpr (LBFFS_HALO_KEEP) {
-                st_hint_v4(sec, quad, pol);
-                st_hint_v4(reinterpret_cast<uint4*>(sec) + 1, quad, pol);
-            } else {
-                reinterpret_cast<uint4*>(sec)[0] = quad;
-                reinterpret_cast<uint4*>(sec)[1] = quad;
-            }
-        } else if constexpr (LBFFS_HALO_KEEP) {
-            if constexpr (sizeof(W) == 2) st_hint_b16(f + dst, v[n], pol);
-            else st_hint_b32(f + dst, v[n], pol);
+            reinterpret_cast<uint4*>(sec)[0] = quad;
+            reinterpret_cast<uint4*>(sec)[1] = quad;
         } else {
             f[dst] = v[n];
         }
@@ -1288,8 +1250,6 @@ __device__ __forceinline__ void halo_cell_rt(W* f, const PadGeom& g, const int (
     const bool face = (bw >> 9) & 1;
     const int N[3] = {g.nx, g.ny, g.nz};
     const int ip = g.porg + x[2] * g.pxy + x[1] * g.px + x[0];
-    [[maybe_unused]] uint64_t pol = 0;
-    if constexpr (LBFFS_HALO_KEEP) pol = l2_policy_evict_last();
     W v[NQ];
 #pragma unroll
     for (int n = 0; n < NQ; n++) {
@@ -1310,10 +1270,7 @@ __device__ __forceinline__ void halo_cell_rt(W* f, const PadGeom& g, const int (
         }
         const int src_q = miss ? halo_missing<Q>(dq, bcode) : q;
         const int src_i = miss ? ip : g.porg + up[2] * g.pxy + up[1] * g.px + up[0];
-        const W* src = f + (long long)src_q * g.pE + src_i;
-        if constexpr (!LBFFS_HALO_KEEP) v[n] = __ldg(src);
-        else if constexpr (sizeof(W) == 2) v[n] = ld_hint_b16(src, pol);
-        else v[n] = ld_hint_b32(src, pol);
+        v[n] = __ldg(f + (long long)src_q * g.pE + src_i);
     }
     // an x ghost sits alone in the padding sector before / after its row: writing the whole
     // 32-byte sector avoids a read-modify-write of a partly written sector
@@ -1328,16 +1285,8 @@ __device__ __forceinline__ void halo_cell_rt(W* f, const PadGeom& g, const int (
             W* sec = f + (HI ? dst : dst - (A - 1));
             const uint32_t w32 = sizeof(W) == 4 ? (uint32_t)v[n] : ((uint32_t)v[n] | ((uint32_t)v[n] << 16));
             const uint4 quad = make_uint4(w32, w32, w32, w32);
-            if constexpr (LBFFS_HALO_KEEP) {
-                st_hint_v4(sec, quad, pol);
-                st_hint_v4(reinterpret_cast<uint4*>(sec) + 1, quad, pol);
-            } else {
-                reinterpret_cast<uint4*>(sec)[0] = quad;
-                reinterpret_cast<uint4*>(sec)[1] = quad;
-            }
-        } else if constexpr (LBFFS_HALO_KEEP) {
-            if constexpr (sizeof(W) == 2) st_hint_b16(f + dst, v[n], pol);
-            else st_hint_b32(f + dst, v[n], pol);
+            reinterpret_cast<uint4*>(sec)[0] = quad;
+            reinterpret_cast<uint4*>(sec)[1] = quad;
         } else {
             f[dst] = v[n];
         }
