@@ -69,8 +69,11 @@ cudaError_t lbffs::ctx_alloc_bytes(lbffs_ctx* c, void** p, size_t bytes)
         if (!*p) return cudaErrorMemoryAllocation;
         return cudaMemsetAsync(*p, 0, bytes, c->stream);
     }
+    // zeroed on the context's stream: the context's streams are non-blocking, so a memset on the
+    // legacy default stream would not be ordered before the kernels that fill the buffer next
+    // (a special list built right after its allocation was intermittently zeroed under it)
     cudaError_t e = cudaMalloc(p, bytes);
-    if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, bytes, c->stream);
     return e;
 }
 

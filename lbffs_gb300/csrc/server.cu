@@ -613,7 +613,10 @@ extern "C" int lbffs_server_create(const lbffs_server_desc* desc, lbffs_server**
     if (e == cudaSuccess) e = cudaMalloc(&s->stage, sizeof(float) * s->stage_elems);
     if (e == cudaSuccess) e = cudaMalloc(&s->stage2, sizeof(float) * s->stage_elems);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_done, sizeof(long long) * desc->max_cases);
-    if (e == cudaSuccess) e = cudaMemset(s->d_done, 0, sizeof(long long) * desc->max_cases);
+    // zeroed on a server stream and waited for (the streams are non-blocking: a legacy-stream
+    // memset would not be ordered before their first launches)
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_done, 0, sizeof(long long) * desc->max_cases, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_done, sizeof(long long) * desc->max_cases);
     if (e != cudaSuccess) {
         const std::string m = std::string("lbffs_server_create: ") + cudaGetErrorString(e);
