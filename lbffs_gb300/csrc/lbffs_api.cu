@@ -793,7 +793,7 @@ extern "C" int lbffs_set_markers(lbffs_ctx* c, const float* xyz, int n)
     CK(ensure_g(c));
     CK(dalloc(c, &c->markers, (size_t)3 * n));
     CK(dalloc(c, &c->gm, (size_t)3 * n));
-    CK(cudaMemcpy(c->markers, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(c->markers, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
     if (!c->ibm_acc) CK(dalloc(c, &c->ibm_acc, (size_t)3 * c->E));
     if (!c->ibm_lag) CK(dalloc(c, &c->ibm_lag, 3));
     if (!c->ibm_box) CK(dalloc(c, &c->ibm_box, 12));
