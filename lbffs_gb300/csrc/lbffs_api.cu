@@ -408,6 +408,24 @@ static int commit(lbffs_ctx* c)
     return LBFFS_OK;
 }
 
+// Population q of an FP32 context between the reference's dense host layout (f[q * E + ic]) and
+// the padded device planes of the current copy (upload: into copy 0), as one pitched 3-D copy:
+// rows of nx floats, the device rows px apart and its planes pxy apart.
+static cudaError_t copy_plane_f32(lbffs_ctx* c, int q, const float* host_in, bool upload)
+{
+    const PadGeom& g = c->pg;
+    float* dev = static_cast<float*>(upload ? c->f[0] : c->f[c->fcur]) + (size_t)q * (size_t)g.pE + g.porg;
+    float* h = const_cast<float*>(host_in) + (size_t)q * (size_t)c->E;
+    cudaMemcpy3DParms p = {};
+    const cudaPitchedPtr dp = make_cudaPitchedPtr(dev, (size_t)g.px * sizeof(float), (size_t)g.nx, (size_t)g.ny + 2);
+    const cudaPitchedPtr hp = make_cudaPitchedPtr(h, (size_t)g.nx * sizeof(float), (size_t)g.nx, (size_t)g.ny);
+    p.srcPtr = upload ? hp : dp;
+    p.dstPtr = upload ? dp : hp;
+    p.extent = make_cudaExtent((size_t)g.nx * sizeof(float), (size_t)g.ny, (size_t)g.nz);
+    p.kind = upload ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    return cudaMemcpy3DAsync(&p, c->stream);
+}
+
 extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t bytes)
 {
     if (!c || !host) return fail(c, LBFFS_E_ARG, "lbffs_upload: null argument");
@@ -427,6 +445,15 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
         const float* h = static_cast<const float*>(host);
         // both population copies get the uploaded values: initialization.hpp fills f and fTmp alike, and
         // cells that are never written (solid cells) must read the same values from either copy
+        if (c->d.storage == LBFFS_FP32) {
+            // FP32 is stored as is: one pitched copy per direction into the padded planes, then the
+            // second copy device to device (no staging, no conversion kernel)
+            for (int q = 0; q < c->Q; q++) CK(copy_plane_f32(c, q, h, true));
+            CK(cudaMemcpyAsync(c->f[1], c->f[0], (size_t)c->Q * (size_t)c->pg.pE * sizeof(float),
+                               cudaMemcpyDeviceToDevice, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            return LBFFS_OK;
+        }
         for (long long r = 0; r < rows; r += chunk) {
             const long long n = (rows - r < chunk) ? rows - r : chunk;
             CK(cudaMemcpyAsync(c->stage, h + r * nx, (size_t)(n * nx) * sizeof(float), cudaMemcpyHostToDevice,
@@ -465,6 +492,11 @@ extern "C" int lbffs_download(lbffs_ctx* c, int field, void* host, size_t bytes)
         const long long nx = c->d.nx;
         const long long rows = (long long)c->Q * c->d.ny * c->d.nz, chunk = (long long)c->stage_elems / nx;
         float* h = static_cast<float*>(host);
+        if (c->d.storage == LBFFS_FP32) {
+            for (int q = 0; q < c->Q; q++) CK(copy_plane_f32(c, q, h, false));
+            CK(cudaStreamSynchronize(c->stream));
+            return LBFFS_OK;
+        }
         for (long long r = 0; r < rows; r += chunk) {
             const long long n = (rows - r < chunk) ? rows - r : chunk;
             CK(decode_f(c->d.storage, c->Q, c->f[c->fcur], c->stage, r, n, c->pg, c->stream));
