@@ -20,11 +20,11 @@ struct BatchCase {
 
 // x segments one bulk tile covers (BULK_V per warp of a BULK_BX-thread CTA; bulk_segments)
 constexpr int BATCH_SEG_PER_TILE = (BULK_BX / 32) * BULK_V;
-// bulk tiles one CTA of the batched kernel runs (one case's argument copy serves them all); a
-// build-time tuning value.  On the 48-request served sample 4 measured best (GPU busy time
-// 1.818 s; 1: 1.859 s, 2: 1.815 s, 8: 1.845 s).
+// bulk tiles one CTA of the batched kernel runs (consecutive tiles of one case); a build-time
+// tuning value.  On the 48-request served sample 2 measured best (GPU busy time 1.680 s; 4: 1.688 s,
+// 8: 1.717 s; with the shared-memory argument copy 1: 1.859 s).
 #ifndef LBFFS_BATCH_TILES
-#define LBFFS_BATCH_TILES 4
+#define LBFFS_BATCH_TILES 2
 #endif
 constexpr int BATCH_TILES_PER_CTA = LBFFS_BATCH_TILES;
 
