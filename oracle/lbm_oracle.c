@@ -77,7 +77,10 @@ typedef struct or_config {
     int wall;      /* WALL_BB or WALL_IBB */
     int collision; /* COLL_RR or COLL_CUMULANT */
     real cs;       /* Smagorinsky constant */
+    int damping;   /* DAMP_WALL (the reference's live factor), DAMP_VAN_DRIEST or DAMP_NONE */
 } or_config;
+
+enum { DAMP_WALL = 0, DAMP_VAN_DRIEST = 1, DAMP_NONE = 2 };
 
 typedef struct lat {
     int Q;
@@ -410,8 +413,28 @@ static void internal_wall(const ctx* X, real* ft, const real* f, const long* up,
     }
 }
 
+/* Van Driest damped mixing length kappa * y * (1 - exp(-y+ / A+)) of the block the reference keeps
+ * commented out in smagorinskyTauSGS (D3Q19 kernel.cl:2178-2197, D3Q27 kernel.cl:2072-2091): y+ from
+ * the log law u+ = ln(E y+) / kappa with the cell's own speed |u| at wall distance y, by the
+ * reference's fixed-point iteration y+ <- (kappa |u| y / nu + y+) / (1 + ln(E y+)) from y+ = 1, at
+ * most 10 iterations, stopping when y+ changes by at most 0.001; kappa 0.41, A+ 26, E 9.8.  The
+ * eddy viscosity is scaled by min(1, length / Cs)^2; this returns length / Cs. */
+static real van_driest_ratio(real y, real umag, real nu, real cs)
+{
+    const real kappa = (real)0.41, Aplus = (real)26, Ek = (real)9.8;
+    real yp = 1, ypn;
+    int it = 0;
+    do {
+        ypn = yp;
+        yp = (kappa * umag * y / nu + yp) / ((real)1 + (real)log((double)(Ek * yp)));
+        it++;
+    } while ((real)fabs((double)(yp - ypn)) > (real)0.001 && it < 10);
+    return (kappa / cs) * (((real)1 + (real)1e-10) - (real)exp((double)(-yp / Aplus))) * y;
+}
+
 /* smagorinskyTauSGS (D3Q19 kernel.cl:2133-2201): eddy relaxation time from |Pi_neq| with the
- * min(1, kappa y / Cs)^2 near-wall damping (y = sdf when one is set). */
+ * min(1, kappa y / Cs)^2 near-wall damping (y = sdf when one is set), or the Van Driest damping
+ * above, or none. */
 static real smagorinsky(const ctx* X, const real* ft, real rho, real u, real v, real w, real omega, real sdf)
 {
     const lat* L = &X->L;
@@ -431,8 +454,13 @@ static real smagorinsky(const ctx* X, const real* ft, real rho, real u, real v, 
     real cs = X->cfg->cs;
     real t = X->p->LES * (real)0.5 *
              (-tau + (real)sqrt((double)(tau * tau + (real)18 * (real)sqrt(2.0) * cs * cs * spp / rho)));
-    if (sdf != (real)10000 && sdf > 0) {
-        real d = (real)0.41 * sdf / cs;
+    if (sdf != (real)10000 && sdf > 0 && X->cfg->damping != DAMP_NONE) {
+        real d;
+        if (X->cfg->damping == DAMP_VAN_DRIEST) {
+            d = van_driest_ratio(sdf, (real)sqrt((double)usq), (tau - (real)0.5) / (real)3, cs);
+        } else {
+            d = (real)0.41 * sdf / cs;
+        }
         if (d > 1) d = 1;
         t *= d * d;
     }
@@ -668,6 +696,33 @@ static void init_ctx(ctx* X, const or_config* cfg, const or_params* p, or_fields
 }
 
 int oracle_q_real_bytes(void) { return (int)sizeof(real); }
+
+/* One collision of one cell, for the tests that check the collision operators on their own:
+ * ft -> out with the cell's rho and velocity (u including the half-force shift, as the step passes
+ * it), molecular relaxation time tau and eddy part tau_sgs.  collision: COLL_RR or COLL_CUMULANT
+ * (D3Q27 only). */
+int oracle_collide(int q, int collision, const real* ft, real rho, real u, real v, real w, real tau, real tau_sgs,
+                   real omegaB, real dpdx, real clim, real* out)
+{
+    if (q != 19 && q != 27) return -1;
+    if (q == 19 && collision != COLL_RR) return -1;
+    or_config cfg = {q, SGS_SMAG, WALL_BB, collision, (real)0.1, DAMP_WALL};
+    or_params p;
+    memset(&p, 0, sizeof p);
+    p.nx = p.ny = p.nz = 1;
+    p.dpdx = dpdx;
+    p.omegaB = omegaB;
+    p.clim = clim;
+    ctx X;
+    memset(&X, 0, sizeof X);
+    X.cfg = &cfg;
+    X.p = &p;
+    make_lat(&X.L, q);
+    if (q == 19) collide_rr19(&X, out, ft, rho, u - (real)0.5 * dpdx / rho, v, w, tau, tau_sgs);
+    else if (collision == COLL_CUMULANT) collide_cumulant27(&X, out, ft, rho, u, v, w, tau, tau_sgs);
+    else collide_rr27(&X, out, ft, rho, u - (real)0.5 * dpdx / rho, v, w, tau, tau_sgs);
+    return 0;
+}
 
 /* Runs nsteps steps; on return a->f points at the newest populations. */
 int oracle_step(const or_config* cfg, or_fields* a, const or_params* p, const or_ibm* ibm, int nsteps)

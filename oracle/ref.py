@@ -42,9 +42,12 @@ class RefSolver:
             raise FileNotFoundError(path)
         return C.CDLL(path)
 
-    def __init__(self, case, sgs="smag", wall="bb", real="f32", nthreads=0, collision="cumulant", cs=0.1):
+    def __init__(self, case, sgs="smag", wall="bb", real="f32", nthreads=0, collision="cumulant", cs=0.1,
+                 damping="wall"):
+        if damping != "wall" and type(self) is RefSolver:
+            raise ValueError("the reference kernels apply only the live near-wall damping (damping='wall')")
         self.lib = self._load(case, sgs, wall, real)
-        self.sgs, self.wall, self.collision, self.cs = sgs, wall, collision, cs
+        self.sgs, self.wall, self.collision, self.cs, self.damping = sgs, wall, collision, cs, damping
         self.real = np.float32 if real == "f32" else np.float64
         rt = C.c_float if real == "f32" else C.c_double
         self.rt = rt
@@ -148,6 +151,7 @@ ORACLE_DIR = HERE
 SGS = {"smag": 0, "wale": 1}
 WALL = {"bb": 0, "ibb": 1}
 COLLISION = {"rr": 0, "cumulant": 1}
+DAMPING = {"wall": 0, "vandriest": 1, "none": 2}
 
 
 def oracle_available(real="f32"):
@@ -158,8 +162,10 @@ class OracleSolver(RefSolver):
     """Same interface as :class:`RefSolver`, driven by the CPU restatement ``lbm_oracle.c``.
 
     ``collision`` selects the D3Q27 operator ("cumulant" as the reference runs, or "rr");
-    D3Q19 always uses the recursive-regularised operator.  IBM motion may add a sinusoidal
-    displacement (``set_motion``).
+    D3Q19 always uses the recursive-regularised operator.  ``damping`` selects the near-wall
+    damping of the Smagorinsky eddy viscosity: "wall" (the reference's live min(1, kappa y / Cs)^2),
+    "vandriest" (the reference's commented Van Driest block) or "none".  IBM motion may add a
+    sinusoidal displacement (``set_motion``).
     """
 
     def _load(self, case, sgs, wall, real):
@@ -172,14 +178,15 @@ class OracleSolver(RefSolver):
         rt = self.rt
 
         class Config(C.Structure):
-            _fields_ = [("q", C.c_int), ("sgs", C.c_int), ("wall", C.c_int), ("collision", C.c_int), ("cs", rt)]
+            _fields_ = [("q", C.c_int), ("sgs", C.c_int), ("wall", C.c_int), ("collision", C.c_int), ("cs", rt),
+                        ("damping", C.c_int)]
 
         class Motion(C.Structure):
             _fields_ = [("ampX", rt), ("ampY", rt), ("ampZ", rt), ("period", rt), ("step", C.c_long)]
 
         self._Config, self._Motion = Config, Motion
         self.cfg = Config(self.q if hasattr(self, "q") else 0, SGS[self.sgs], WALL[self.wall],
-                          COLLISION[self.collision], self.cs)
+                          COLLISION[self.collision], self.cs, DAMPING[self.damping])
         self.motion = Motion(0, 0, 0, 0, 0)
         self.lib.oracle_step_motion.argtypes = [C.POINTER(Config), C.POINTER(self._Fields), C.POINTER(self._Params),
                                                 C.POINTER(self._Ibm), C.POINTER(Motion), C.c_int]
@@ -190,3 +197,19 @@ class OracleSolver(RefSolver):
     def _call(self, F, P, ibm_p, n):
         self.cfg.q = self.q
         return self.lib.oracle_step_motion(C.byref(self.cfg), C.byref(F), C.byref(P), ibm_p, C.byref(self.motion), n)
+
+
+def collide(q, ft, rho, u, v, w, tau, tau_sgs=0.0, omega_b=0.1, dpdx=0.0, clim=0.01, collision="rr", real="f64"):
+    """One collision of one cell through the oracle's operator (``oracle_collide``): the populations
+    after collision for pre-collision populations ft (u including the half-force shift)."""
+    lib = C.CDLL(os.path.join(ORACLE_DIR, f"liboracle_{real}.so"))
+    rt = C.c_float if real == "f32" else C.c_double
+    dt = np.float32 if real == "f32" else np.float64
+    lib.oracle_collide.argtypes = [C.c_int, C.c_int, C.c_void_p] + [rt] * 9 + [C.c_void_p]
+    src = np.ascontiguousarray(ft, dtype=dt)
+    out = np.zeros(q, dt)
+    rc = lib.oracle_collide(q, COLLISION[collision], src.ctypes.data_as(C.c_void_p), rho, u, v, w, tau, tau_sgs,
+                            omega_b, dpdx, clim, out.ctypes.data_as(C.c_void_p))
+    if rc != 0:
+        raise ValueError("oracle_collide: unsupported lattice / operator")
+    return out
