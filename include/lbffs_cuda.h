@@ -56,6 +56,13 @@ enum lbffs_wall {
     LBFFS_WALL_BB = 0, /* half-way bounce-back on STL links (D3Q19 kernel.cl:1947) */
     LBFFS_WALL_IBB = 1 /* Filippova-Hanel / Mei-Luo-Shyy interpolated bounce-back (D3Q27 kernel.cl:1847-1888) */
 };
+/* near-wall damping of the Smagorinsky eddy viscosity (cells with a wall distance sdf, 0 < sdf != 10000) */
+enum lbffs_damping {
+    LBFFS_DAMP_WALL = 0,       /* min(1, kappa y / Cs)^2, kappa 0.41: the reference's live factor (kernel.cl:2170-2176) */
+    LBFFS_DAMP_VAN_DRIEST = 1, /* min(1, (kappa / Cs) (1 - exp(-y+ / 26)) y)^2 with y+ from the log law (9.8 y+ = exp(kappa u+)):
+                                  the block the reference keeps commented out (D3Q19 kernel.cl:2178-2197) */
+    LBFFS_DAMP_NONE = 2        /* no damping */
+};
 
 /* Lattice description; replaces the compile-time choice of D3Q19_opencl vs D3Q27_opencl. */
 typedef struct lbffs_desc {
@@ -67,6 +74,7 @@ typedef struct lbffs_desc {
     int wall;        /* enum lbffs_wall */
     int device;      /* CUDA device ordinal */
     float cs;        /* Smagorinsky constant (the reference's live value is 0.1, kernel.cl:3628) */
+    int damping;     /* enum lbffs_damping (0, the reference's factor, in a zero-initialised descriptor) */
 } lbffs_desc;
 
 /* Field ids: the reference's device buffers (ns.cpp:405-436). */

@@ -27,6 +27,7 @@ STORAGE = {"fp32": FP32, "fp16s": FP16S, "bf16s": BF16S}
 COLLISION = {"rr": 0, "cumulant": 1}
 SGS = {"smag": 0, "smagorinsky": 0, "wale": 1}
 WALL = {"bb": 0, "ibb": 1}
+DAMPING = {"wall": 0, "vandriest": 1, "none": 2}
 FIELDS = {"f": 0, "boundary": 1, "boundary1": 2, "boundary2": 3, "boundary3": 4, "sdf": 5, "solid": 6,
           "nei_solid": 7, "u0": 8, "v0": 9, "w0": 10, "omega": 11, "tau_sgs": 12, "rho": 13, "u": 14, "v": 15,
           "w": 16, "fwx": 17, "fwy": 18, "fwz": 19, "gx": 20, "gy": 21, "gz": 22, "out_rho": 23, "out_u": 24,
@@ -44,7 +45,8 @@ class LbffsError(RuntimeError):
 
 class Desc(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("q", C.c_int), ("storage", C.c_int),
-                ("collision", C.c_int), ("sgs", C.c_int), ("wall", C.c_int), ("device", C.c_int), ("cs", C.c_float)]
+                ("collision", C.c_int), ("sgs", C.c_int), ("wall", C.c_int), ("device", C.c_int), ("cs", C.c_float),
+                ("damping", C.c_int)]
 
 
 class StepParams(C.Structure):
@@ -130,15 +132,17 @@ class Lattice:
     """One device lattice: the C-ABI context plus host-side conveniences.
 
     ``q`` 19 or 27; ``storage`` "fp32" | "fp16s" | "bf16s"; ``collision`` "rr" | "cumulant";
-    ``sgs`` "smag" | "wale"; ``wall`` "bb" | "ibb".
+    ``sgs`` "smag" | "wale"; ``wall`` "bb" | "ibb"; ``damping`` (near-wall damping of the Smagorinsky
+    eddy viscosity) "wall" (the reference's live factor) | "vandriest" | "none".
     """
 
-    def __init__(self, nx, ny, nz, q=19, storage="fp32", collision="rr", sgs="smag", wall="bb", device=0, cs=0.1):
+    def __init__(self, nx, ny, nz, q=19, storage="fp32", collision="rr", sgs="smag", wall="bb", device=0, cs=0.1,
+                 damping="wall"):
         self.lib = load_library()
         self.nx, self.ny, self.nz, self.q = int(nx), int(ny), int(nz), int(q)
         self.E = self.nx * self.ny * self.nz
         d = Desc(self.nx, self.ny, self.nz, self.q, STORAGE[storage], COLLISION[collision], SGS[sgs], WALL[wall],
-                 int(device), float(cs))
+                 int(device), float(cs), DAMPING[damping])
         h = C.c_void_p()
         self._check(self.lib.lbffs_create(C.byref(d), C.byref(h)), None)
         self.h = h

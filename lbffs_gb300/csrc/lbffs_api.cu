@@ -184,6 +184,8 @@ int lbffs::ctx_create(const lbffs_desc* desc, Arena* arena, cudaStream_t stream,
     if (d.sgs != LBFFS_SGS_SMAGORINSKY && d.sgs != LBFFS_SGS_WALE) return fail(c, LBFFS_E_ARG, "lbffs_create: bad sgs");
     if (d.wall != LBFFS_WALL_BB && d.wall != LBFFS_WALL_IBB) return fail(c, LBFFS_E_ARG, "lbffs_create: bad wall");
     if (!(d.cs > 0.f)) return fail(c, LBFFS_E_ARG, "lbffs_create: cs must be > 0");
+    if (d.damping < LBFFS_DAMP_WALL || d.damping > LBFFS_DAMP_NONE)
+        return fail(c, LBFFS_E_ARG, "lbffs_create: bad damping");
     const long long E = (long long)d.nx * d.ny * d.nz;
     if (E >= (1LL << 31)) return fail(c, LBFFS_E_ARG, "lbffs_create: more than 2^31 - 1 cells");
     // padded planes: one ghost cell on every side, rows starting on 32-byte sectors
@@ -378,8 +380,8 @@ static int commit(lbffs_ctx* c)
     CK(setup_pack_bc(c->iarr[0], c->iarr[1], c->iarr[2], c->iarr[3], c->bc, nx, ny, nz, c->stream));
     uint8_t* scratch = nullptr;
     CK(ctx_alloc_bytes(c, (void**)&scratch, E));
-    cudaError_t e = setup_classify(c->Q, c->bc, c->solid, c->nei, c->sdf, c->omega, c->omega0, c->d.cs, c->flags,
-                                   scratch, nx, ny, nz, c->stream);
+    cudaError_t e = setup_classify(c->Q, c->bc, c->solid, c->nei, c->sdf, c->omega, c->omega0, c->d.cs,
+                                   c->d.damping, c->flags, scratch, nx, ny, nz, c->stream);
     cudaStreamSynchronize(c->stream);
     ctx_free(c, scratch);
     CK(e);
@@ -575,6 +577,7 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
     a.spz = p->spz_width;
     a.clim = p->clim;
     a.cs = c->d.cs;
+    a.damping = c->d.damping;
     a.sponge_mask = c->sponge_mask;
     a.sgs = c->d.sgs;
     a.wall = c->d.wall;

@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/lbffs_cuda.h"
+
 namespace lbffs {
 
 // Boundary codes: src/input.hpp:221-256
@@ -195,6 +197,7 @@ struct StepArgs {
     long long E;
     int nx, ny, nz;
     float omega0, dpdx, les, omega_b, spz, clim, cs;
+    int damping;      // near-wall damping of the Smagorinsky eddy viscosity (enum lbffs_damping)
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity
     int store_all;    // store rho/u/v/w/tau for every fluid cell this step
     int bulk_kind;    // D3Q19 bulk kernel: 0 per-thread loads, 1 row-staged bulk copies (launch choice)

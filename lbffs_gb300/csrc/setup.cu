@@ -70,9 +70,11 @@ __global__ void k_classify1(const uint16_t* bc, const uint8_t* solid, const uint
     flags[ic] = fl;
 }
 
-// pass 2: cells next to a special cell store their macroscopics; damping / omega read bits
+// pass 2: cells next to a special cell store their macroscopics; damping / omega read bits.  A cell
+// reads its wall distance when the damping can change its eddy viscosity: the reference's factor
+// min(1, 0.41 y / Cs)^2 only below y = Cs / 0.41, the Van Driest factor wherever a distance is set.
 __global__ void k_classify2(const uint8_t* pass1, uint8_t* flags, const float* sdf, const float* omega, float omega0,
-                            float cs, int nx, int ny, int nz)
+                            float cs, int damping, int nx, int ny, int nz)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx) return;
@@ -99,21 +101,23 @@ __global__ void k_classify2(const uint8_t* pass1, uint8_t* flags, const float* s
     fl &= (FL_SPECIAL | FL_LINK | FL_FACE);
     if (near) fl |= FL_STORE;
     const float s = sdf[ic];
-    if (s != 10000.f && s > 0.f && 0.41f * s / cs < 1.f) fl |= FL_SDF;
+    if (s != 10000.f && s > 0.f &&
+        ((damping == LBFFS_DAMP_WALL && 0.41f * s / cs < 1.f) || damping == LBFFS_DAMP_VAN_DRIEST))
+        fl |= FL_SDF;
     if (__float_as_uint(omega[ic]) != __float_as_uint(omega0)) fl |= FL_OMEGA;
     flags[ic] = fl;
 }
 
 cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
-                           const float* omega, float omega0, float cs, uint8_t* flags, uint8_t* scratch, int nx, int ny,
-                           int nz, cudaStream_t st)
+                           const float* omega, float omega0, float cs, int damping, uint8_t* flags, uint8_t* scratch,
+                           int nx, int ny, int nz, cudaStream_t st)
 {
     const dim3 grid((nx + 127) / 128, ny, nz);
     if (Q == 19) k_classify1<19><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
     else k_classify1<27><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_classify2<<<grid, 128, 0, st>>>(scratch, flags, sdf, omega, omega0, cs, nx, ny, nz);
+    k_classify2<<<grid, 128, 0, st>>>(scratch, flags, sdf, omega, omega0, cs, damping, nx, ny, nz);
     return cudaGetLastError();
 }
 

@@ -99,10 +99,37 @@ __device__ __forceinline__ float smagorinsky(const float (&ft)[Q], float rho, fl
     return les * 0.5f * (-tau + sqrtf(tau * tau + 18.f * 1.41421356237f * cs * cs * sqrtf(pp) / rho));
 }
 
-__device__ __forceinline__ float damping(float t, float sdf, float cs)
+// Van Driest mixing length over Cs, (kappa / Cs) (1 - exp(-y+ / A+)) y, of the block the reference
+// keeps commented out in smagorinskyTauSGS (D3Q19 kernel.cl:2178-2197, D3Q27 kernel.cl:2072-2091):
+// y+ from the log law u+ = ln(E y+) / kappa at wall distance y with the cell's own speed, by the
+// fixed-point iteration y+ <- (kappa |u| y / nu + y+) / (1 + ln(E y+)) from y+ = 1 (at most 10 times,
+// until y+ moves by at most 0.001); kappa 0.41, A+ 26, E 9.8, nu = (tau - 1/2) / 3.  1 + 1e-10 is 1 in
+// FP32, as in the reference's float expression.
+static __device__ __noinline__ float van_driest_ratio(float y, float umag, float nu, float cs)
 {
-    if (sdf != 10000.f && sdf > 0.f) {
-        const float d = fminf(1.f, 0.41f * sdf / cs);
+    const float kappa = 0.41f, Aplus = 26.f, Ek = 9.8f;
+    float yp = 1.f, ypn;
+    int it = 0;
+    do {
+        ypn = yp;
+        yp = (kappa * umag * y / nu + yp) / (1.f + logf(Ek * yp));
+        it++;
+    } while (fabsf(yp - ypn) > 0.001f && it < 10);
+    return (kappa / cs) * (1.f - expf(-yp / Aplus)) * y;
+}
+
+// near-wall damping of the eddy relaxation time t (smagorinskyTauSGS, kernel.cl:2166-2199) for a
+// cell at wall distance sdf with velocity (u, v, w) and relaxation rate omega
+__device__ __forceinline__ float damping(const StepArgs& a, float t, float sdf, float u, float v, float w,
+                                         float omega)
+{
+    if (sdf != 10000.f && sdf > 0.f && a.damping != LBFFS_DAMP_NONE) {
+        float d;
+        if (a.damping == LBFFS_DAMP_VAN_DRIEST)
+            d = van_driest_ratio(sdf, sqrtf(u * u + v * v + w * w), (1.f / omega - 0.5f) / 3.f, a.cs);
+        else
+            d = 0.41f * sdf / a.cs;
+        d = fminf(1.f, d);
         t *= d * d;
     }
     return t;
@@ -277,7 +304,7 @@ __device__ __forceinline__ void bulk_collide(const StepArgs& a, float (&ft)[Q], 
             tsgs = wale_general(a, i, j, k, ic, own);
         } else if constexpr (LES) {
             tsgs = smagorinsky19<HS>(m, u, v, w, omega, a.les, a.cs);
-            if (fl & FL_SDF) tsgs = damping(tsgs, __ldg(a.sdf + ic), a.cs);
+            if (fl & FL_SDF) tsgs = damping(a, tsgs, __ldg(a.sdf + ic), u, v, w, omega);
         }
         if (a.err && !(rho == rho)) atomicOr(a.err, 1);
         const float tau = sponge_tau(a, 1.f / omega, tsgs, i, j, k);
@@ -302,7 +329,7 @@ __device__ __forceinline__ void bulk_collide(const StepArgs& a, float (&ft)[Q], 
         w = m.j[2] * ir;
         if constexpr (LES) {
             tsgs = smag_tau(smag_pp_raw(m.s, rho, u, v, w), rho, omega, a.les, a.cs);
-            if (fl & FL_SDF) tsgs = damping(tsgs, __ldg(a.sdf + ic), a.cs);
+            if (fl & FL_SDF) tsgs = damping(a, tsgs, __ldg(a.sdf + ic), u, v, w, omega);
         }
         if (a.err && !(rho == rho)) atomicOr(a.err, 1);
         const float tau = sponge_tau(a, 1.f / omega, tsgs, i, j, k);
@@ -404,7 +431,8 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], c
         const float rho = lane(m.rho, c);
         if constexpr (LES) {
             tsl[c] = smag_tau(lane(pp, c), rho, oml[c], a.les, a.cs);
-            if (fl[c] & FL_SDF) tsl[c] = damping(tsl[c], __ldg(a.sdf + ic[c]), a.cs);
+            if (fl[c] & FL_SDF)
+                tsl[c] = damping(a, tsl[c], __ldg(a.sdf + ic[c]), lane(u, c), lane(v, c), lane(w, c), oml[c]);
         }
         if (act[c]) {
             if (a.err && !(rho == rho)) atomicOr(a.err, 1);
@@ -1062,7 +1090,7 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     } else if (a.les != 0.f) {
         if constexpr (Q == 19) tsgs = smagorinsky19(m19, u, v, w, omega, a.les, a.cs);
         else tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
-        tsgs = damping(tsgs, a.sdf[ic], a.cs);
+        tsgs = damping(a, tsgs, a.sdf[ic], u, v, w, omega);
     }
     a.rho_n[ic] = rho;
     a.u_n[ic] = u;

@@ -96,6 +96,36 @@ def build(name):
     if name == "wallfn_q27":
         c = make_case(28, 14, 6, 27, _wallfn_faces(), nu=0.004)
         return c, dict(sgs="smag", wall="ibb", collision="cumulant", steps=30, kw={})
+    # ---- D3Q27 recursive regularised collision and Van Driest damping: no reference counterpart, so
+    # these cases are checked against the oracle (FP32 and FP64) only ----
+    if name == "cavity_q27_rr":
+        c = make_case(12, 12, 12, 27, cavity_faces(0.05), nu=0.032)
+        return c, dict(sgs="smag", wall="ibb", collision="rr", steps=60, kw={})
+    if name == "mixed_q27_rr":
+        c = make_case(16, 14, 12, 27, _mixed_faces(), nu=0.02)
+        return c, dict(sgs="smag", wall="ibb", collision="rr", steps=30, kw={})
+    if name == "cylinder_q27_rr_ibb_les_sponge":
+        solid, sdf = cylinder_z(28, 18, 8, 9.2, 8.7, 3.3)
+        c = make_case(28, 18, 8, 27, channel_faces(0.05), nu=0.003, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="ibb", collision="rr", steps=30, kw=dict(LES=1.0, spzWidth=0.2))
+    if name == "step_q27_rr_les":
+        # the backward-facing step at reduced size: walls top and bottom, z periodic, inlet 0.06
+        solid, sdf = backward_step(40, 16, 8, 12, 6)
+        f = channel_faces(0.06, top_bottom=BOUNCEBACK, z_periodic=True)
+        c = make_case(40, 16, 8, 27, f, nu=0.001, solid=solid, sdf=sdf)
+        return c, dict(sgs="smag", wall="ibb", collision="rr", steps=30, kw=dict(LES=1.0, spzWidth=0.25))
+    if name == "step_q27_rr_vandriest":
+        c, run = build("step_q27_rr_les")
+        run["damping"] = "vandriest"
+        return c, run
+    if name == "step_q19_les_vandriest":
+        c, run = build("step_q19_les")
+        run["damping"] = "vandriest"
+        return c, run
+    if name == "bluff_q27_rr_les_ibm":
+        c, run = build("bluff_q27_les_ibm")
+        run["collision"] = "rr"
+        return c, run
     raise KeyError(name)
 
 
@@ -104,6 +134,12 @@ REFERENCE_CASES = ["cavity_q19", "cavity_q19_les", "cavity_q19_wale", "cylinder_
                    "cylinder2d_q19_ibb", "mixed_q19", "density_q19_dpdx", "step_q19_les", "mixed_q27_cumulant",
                    "cylinder_q27_cumulant_les", "cavity_q27_wale", "ibm_q19", "wallfn_q19", "wallfn_q27",
                    "bluff_q27_les_ibm"]
+
+
+# cases with no reference counterpart (D3Q27 RR, Van Driest damping): checked against the oracle in
+# FP32 and FP64
+ORACLE_CASES = ["cavity_q27_rr", "mixed_q27_rr", "cylinder_q27_rr_ibb_les_sponge", "step_q27_rr_les",
+                "step_q27_rr_vandriest", "step_q19_les_vandriest", "bluff_q27_rr_les_ibm"]
 
 
 def rel_err(a, b):

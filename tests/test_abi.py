@@ -28,7 +28,7 @@ def test_create_rejects_bad_descriptors_without_gpu_calls(cuda_lib):
     h = ctypes.c_void_p()
     for bad in (L.Desc(0, 4, 4, 19, 0, 0, 0, 0, 0, 0.1), L.Desc(4, 4, 4, 23, 0, 0, 0, 0, 0, 0.1),
                 L.Desc(4, 4, 4, 19, 0, 1, 0, 0, 0, 0.1), L.Desc(4, 4, 4, 19, 7, 0, 0, 0, 0, 0.1),
-                L.Desc(4, 4, 4, 19, 0, 0, 0, 0, 0, 0.0)):
+                L.Desc(4, 4, 4, 19, 0, 0, 0, 0, 0, 0.0), L.Desc(4, 4, 4, 19, 0, 0, 0, 0, 0, 0.1, 3)):
         assert lib.lbffs_create(ctypes.byref(bad), ctypes.byref(h)) == L.E_ARG
         assert lib.lbffs_last_error(None)
 

@@ -23,7 +23,7 @@ def run_gpu(name, storage="fp32", steps=None, store_fields=2, c=None, run=None):
     if c is None:
         c, run = build(name)
     lat = L.Lattice(c.nx, c.ny, c.nz, q=c.q, storage=storage, collision=run["collision"], sgs=run["sgs"],
-                    wall=run["wall"])
+                    wall=run["wall"], damping=run.get("damping", "wall"))
     lat.load_case(c)
     if "markers" in run:
         lat.set_markers(run["markers"])
@@ -38,7 +38,8 @@ def run_gpu(name, storage="fp32", steps=None, store_fields=2, c=None, run=None):
 def run_oracle(name, real="f32", steps=None):
     from oracle import ref as R
     c, run = build(name)
-    o = R.OracleSolver(c, sgs=run["sgs"], wall=run["wall"], collision=run["collision"], real=real)
+    o = R.OracleSolver(c, sgs=run["sgs"], wall=run["wall"], collision=run["collision"], real=real,
+                       damping=run.get("damping", "wall"))
     if "markers" in run:
         o.set_ibm(run["markers"], *run["motion"]["trans"], rot=(0.0, 0.0, 0.0), axis=(0.0, 0.0, 1.0), rot_omega=0.0)
     o.step(steps or run["steps"], **run["kw"])
@@ -126,10 +127,12 @@ def test_fp16s_velocity_error_vs_fp64_oracle(cuda_lib, oracle_built):
     assert out["bf16s"] < 5e-2, out
 
 
-@pytest.mark.parametrize("name", ["bluff_q27_les_ibm", "step_q19_les", "wallfn_q19"])
+@pytest.mark.parametrize("name", ["bluff_q27_les_ibm", "step_q19_les", "wallfn_q19", "bluff_q27_rr_les_ibm",
+                                  "step_q27_rr_les", "step_q27_rr_vandriest", "cylinder_q27_rr_ibb_les_sponge"])
 def test_fp16s_boundary_cases_vs_fp64_oracle(cuda_lib, oracle_built, name):
-    """FP16S storage on the reduced bluff body (D3Q27, IBB, LES, IBM), the LES backward-facing step
-    and the wall-function channel: relative L2 velocity error against the FP64 oracle <= 1e-3."""
+    """FP16S storage on the reduced bluff body (D3Q27, IBB, LES, IBM; cumulant and RR), the LES
+    backward-facing step (D3Q19, and D3Q27 RR with either damping), the D3Q27 RR cylinder channel and the
+    wall-function channel: relative L2 velocity error against the FP64 oracle <= 1e-3."""
     c, run = build(name)
     o = run_oracle(name, real="f64")
     fluid = c.solid == 0
