@@ -343,7 +343,8 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
     ms = e0.elapsed_time(e1)
     counts = lat.cell_counts()
     out = {"ms_per_step": ms / steps, "cells": c.elements, "fluid": counts["fluid"], "special": counts["special"],
-           # k_halo (ghost layer) + k_bulk every step, k_special when the case has special cells
+           # k_bulk every step, k_special when the case has special cells, the ghost fill when the step
+           # does not pull across the border itself (refined by the timing pass's launch counts)
            "launches_per_step": (3 if counts["special"] > 0 else 2) + (4 if sel.get("markers") is not None else 0),
            "lat": lat, "case": c, "sel": sel, "setup": setup}
     if timing_pass:
@@ -355,6 +356,9 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
         i_ms, ni = lat.kernel_time("ibm")
         lat.set_timing(False)
         out["ibm_ms"] = i_ms / max(ni, 1)
+        # launches of the library's kernels per step: bulk, boundary, ghost fill (none when the step pulls
+        # across the border itself), IBM sub-step (four kernels)
+        out["launches_per_step"] = (n + nsp + nh + 4 * ni) / steps
         out["bulk_ms"] = bulk_ms / max(n, 1)
         out["special_ms"] = sp_ms / max(nsp, 1)
         out["halo_ms"] = h_ms / max(nh, 1)
@@ -582,7 +586,7 @@ def main():
                                              "k_halo": res["halo_ms"]}},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": res["launches_per_step"] * args.steps,
+            "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
             "variants": variants,
             "serving": serving,
         }

@@ -317,6 +317,205 @@ __device__ __forceinline__ void moments_to_pop27(float (&M)[3][3][3], float u, f
     for (int q = 0; q < 27; q++) f[q] = P[lat_c(27, q, 0) + 1][lat_c(27, q, 1) + 1][lat_c(27, q, 2) + 1];
 }
 
+// ---- D3Q27 recursive regularised collision in moment form (bulk cells) ----
+// The populations are held as in collide_rr19m (f_q, or g_q = HS (f_q - w_q) for shifted storage), one
+// cell (float) or two (F2).  The moments come from the 13 opposite pairs (q, q + 1 for odd q) into the
+// same Mom19T record the D3Q19 path uses, always in deviation form: r = sum of (f_q - w_q) (times HS),
+// that is rho - 1, and s = sum c_a c_b (f_q - w_q), from which the second-order stress follows without
+// the cancellation of two O(1/3) terms.  Held f (DEV = false, FP32 storage) is shifted per opposite
+// pair (a_p - 2 w_p, exact when a_p lies within a factor two of 2 w_p); rho itself is the direct sum.
+template <bool DEV, int HS = 1, class V = float>
+__device__ __forceinline__ Mom19T<V> moments27p(const V (&f)[27])
+{
+    V a[14], d[14];
+#pragma unroll
+    for (int p = 1; p < 14; p++) {
+        a[p] = f[2 * p - 1] + f[2 * p];
+        d[p] = f[2 * p - 1] - f[2 * p];
+    }
+    Mom19T<V> m;
+    // rest, axis pairs, edge pairs, corner pairs
+    const V tot = ((f[0] + (a[1] + a[2])) + (a[3] + (a[4] + a[5]))) +
+                  (((a[6] + a[7]) + (a[8] + a[9])) + ((a[10] + a[11]) + (a[12] + a[13])));
+    if constexpr (DEV) {
+        m.r = tot;
+        if constexpr (HS == 1) m.rho = 1.f + m.r;
+        else m.rho = 1.f + m.r * (1.f / HS);
+    } else {
+        static_assert(HS == 1, "f held unscaled");
+        m.rho = tot;
+        m.r = tot - 1.f;
+#pragma unroll
+        for (int p = 1; p < 14; p++) a[p] = a[p] - 2.f * lat_w(27, 2 * p - 1);
+    }
+#pragma unroll
+    for (int x = 0; x < 3; x++) {
+        V jx = d[x + 1];  // the axis pair of x comes first (q = 2x + 1)
+#pragma unroll
+        for (int p = 4; p < 14; p++) {
+            const int c = lat_c(27, 2 * p - 1, x);
+            if (c > 0) jx = jx + d[p];
+            else if (c < 0) jx = jx - d[p];
+        }
+        m.j[x] = jx;
+#pragma unroll
+        for (int y = x; y < 3; y++) {
+            V s;
+            bool first = true;
+#pragma unroll
+            for (int p = 1; p < 14; p++) {
+                const int cc = lat_c(27, 2 * p - 1, x) * lat_c(27, 2 * p - 1, y);
+                if (cc == 0) continue;
+                if (first) {
+                    s = cc > 0 ? a[p] : neg(a[p]);
+                    first = false;
+                } else if (cc > 0) {
+                    s = s + a[p];
+                } else {
+                    s = s - a[p];
+                }
+            }
+            m.s[x][y] = m.s[y][x] = s;
+        }
+    }
+    return m;
+}
+
+// The D3Q27 recursive regularised collision (the same operator as collide_rr27) from the moments, for
+// held populations: U without the half-force shift, ir1 = 1 / rho.  FOUT: the results are f_q (FP32
+// storage), else HS (f_q - w_q).  Post-collision populations are the tensor Hermite expansion
+// f_q = w_q rho sum_{abc} H_abc h_a(c_x) h_b(c_y) h_c(c_z) with the 1-D basis h = (1, 3c, 9/2 (c^2 - 1/3))
+// and weights (1/6, 2/3, 1/6): H_000 = 1, H_1 = U (the pressure-gradient source 3 rho w_q c_x dpdx is
+// dpdx added to H_100), H_2 = R2 (bulk / shear split), every higher coefficient = its u-products +
+// (1 - omega) times its recursive non-equilibrium part.  The held output HS (f_q - w_q) takes rho - 1 = r
+// in place of rho H_000.  Each coefficient is scaled by rho HS and by (1/6, 1/2, 1/2) per axis for its
+// order (0, 1, 2) along the axis, so that each 1-D pass of the expansion is P(+-1) = T_0 + T_2 +- T_1,
+// P(0) = 4 T_0 - 2 T_2.
+template <int HS = 1, bool FOUT = false, class V = float>
+__device__ __forceinline__ void collide_rr27p(V (&f)[27], const Mom19T<V>& m, const V (&U)[3], V we, V ir1,
+                                              float omega_b, float dpdx)
+{
+    const float third = 1.f / 3.f;
+    const V k1 = 1.f - we, nwe = neg(we);
+    V ir;
+    if constexpr (HS == 1) ir = ir1;
+    else ir = ir1 * (1.f / HS);
+    const V r3 = m.r * third;
+    const V NU[3] = {neg(U[0]), neg(U[1]), neg(U[2])};
+    V N2[3][3], R2[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = a; b < 3; b++) {
+            const V m2 = (a == b) ? (m.s[a][a] - r3) * ir : m.s[a][b] * ir;
+            N2[a][b] = N2[b][a] = mad(NU[a], U[b], m2);
+            R2[a][b] = R2[b][a] = m2;
+        }
+    const V wm = (omega_b - we) * third;
+    const V wn = wm * (N2[0][0] + N2[1][1] + N2[2][2]);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        R2[a][a] = R2[a][a] - mad(we, N2[a][a], wn);
+#pragma unroll
+        for (int b = a + 1; b < 3; b++) R2[a][b] = R2[b][a] = mad(nwe, N2[a][b], R2[a][b]);
+    }
+    const V u = U[0], v = U[1], w = U[2];
+    const V uu = u * u, vv = v * v, ww = w * w, uv = u * v, uw = u * w, vw = v * w;
+    // A = (1 - omega) N2, D = 2 A (off-diagonal), B_aa = u_a^2 + A_aa
+    const V Axy = k1 * N2[0][1], Axz = k1 * N2[0][2], Ayz = k1 * N2[1][2];
+    const V Dxy = Axy + Axy, Dxz = Axz + Axz, Dyz = Ayz + Ayz;
+    const V Ayy = k1 * N2[1][1], Azz = k1 * N2[2][2];
+    const V Bxx = mad(k1, N2[0][0], uu), Byy = mad(k1, N2[1][1], vv), Bzz = mad(k1, N2[2][2], ww);
+    // third order (x^2 y, ...; xyz)
+    const V H210 = mad(Bxx, v, Dxy * u), H201 = mad(Bxx, w, Dxz * u);
+    const V H120 = mad(Byy, u, Dxy * v), H021 = mad(Byy, w, Dyz * v);
+    const V H102 = mad(Bzz, u, Dxz * w), H012 = mad(Bzz, v, Dyz * w);
+    const V H111 = mad(uv + Axy, w, mad(Axz, v, Ayz * u));
+    // fourth order
+    const V H220 = mad(Bxx, vv, mad(Ayy, uu, (Dxy + Dxy) * uv));
+    const V H202 = mad(Bxx, ww, mad(Azz, uu, (Dxz + Dxz) * uw));
+    const V H022 = mad(Byy, ww, mad(Azz, vv, (Dyz + Dyz) * vw));
+    const V H211 = mad(Bxx, vw, mad(Dxy, uw, mad(Dxz, uv, Ayz * uu)));
+    const V H121 = mad(Byy, uw, mad(Dxy, vw, mad(Dyz, uv, Axz * vv)));
+    const V H112 = mad(Bzz, uv, mad(Dxz, vw, mad(Dyz, uw, Axy * ww)));
+    // fifth and sixth order
+    const V H221 = mad(w, H220, mad(Dxz, u * vv, Dyz * (uu * v)));
+    const V H212 = mad(v, H202, mad(Dxy, u * ww, Dyz * (uu * w)));
+    const V H122 = mad(u, H022, mad(Dxy, v * ww, Dxz * (vv * w)));
+    const V H222 = mad(ww, H220, uv * mad(Azz, uv, (mad(Dxz, vw, Dyz * uw)) * 2.f));
+    // scaled coefficients T[a][b][c]
+    const V rho = m.rho;
+    const V s2 = rho * (HS / 72.f), s1 = rho * (HS / 24.f), s0 = rho * (HS / 8.f);
+    V T[3][3][3];
+    if constexpr (FOUT) T[0][0][0] = m.rho * (1.f / 216.f);
+    else T[0][0][0] = m.r * (1.f / 216.f);
+    T[1][0][0] = (u + dpdx) * s2;
+    T[0][1][0] = v * s2;
+    T[0][0][1] = w * s2;
+    T[2][0][0] = R2[0][0] * s2;
+    T[0][2][0] = R2[1][1] * s2;
+    T[0][0][2] = R2[2][2] * s2;
+    T[1][1][0] = R2[0][1] * s1;
+    T[1][0][1] = R2[0][2] * s1;
+    T[0][1][1] = R2[1][2] * s1;
+    T[2][1][0] = H210 * s1;
+    T[2][0][1] = H201 * s1;
+    T[1][2][0] = H120 * s1;
+    T[0][2][1] = H021 * s1;
+    T[1][0][2] = H102 * s1;
+    T[0][1][2] = H012 * s1;
+    T[2][2][0] = H220 * s1;
+    T[2][0][2] = H202 * s1;
+    T[0][2][2] = H022 * s1;
+    T[1][1][1] = H111 * s0;
+    T[2][1][1] = H211 * s0;
+    T[1][2][1] = H121 * s0;
+    T[1][1][2] = H112 * s0;
+    T[2][2][1] = H221 * s0;
+    T[2][1][2] = H212 * s0;
+    T[1][2][2] = H122 * s0;
+    T[2][2][2] = H222 * s0;
+    // the three 1-D passes; index 0 / 1 / 2 of a finished axis is c = 0 / +1 / -1
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const V e = T[0][b][c] + T[2][b][c];
+            const V p0 = mad(T[0][b][c], 4.f, T[2][b][c] * (-2.f));
+            const V p1 = e + T[1][b][c];
+            T[2][b][c] = e - T[1][b][c];
+            T[1][b][c] = p1;
+            T[0][b][c] = p0;
+        }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const V e = T[a][0][c] + T[a][2][c];
+            const V p0 = mad(T[a][0][c], 4.f, T[a][2][c] * (-2.f));
+            const V p1 = e + T[a][1][c];
+            T[a][2][c] = e - T[a][1][c];
+            T[a][1][c] = p1;
+            T[a][0][c] = p0;
+        }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const V e = T[a][b][0] + T[a][b][2];
+            const V p0 = mad(T[a][b][0], 4.f, T[a][b][2] * (-2.f));
+            const V p1 = e + T[a][b][1];
+            T[a][b][2] = e - T[a][b][1];
+            T[a][b][1] = p1;
+            T[a][b][0] = p0;
+        }
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+        const int cx = lat_c(27, q, 0), cy = lat_c(27, q, 1), cz = lat_c(27, q, 2);
+        f[q] = T[cx < 0 ? 2 : cx][cy < 0 ? 2 : cy][cz < 0 ? 2 : cz];
+    }
+}
+
 // D3Q27 recursive regularised collision on the tensor Hermite basis; U without the half-force shift.
 __device__ __forceinline__ void rr27_closure(float (&f)[27], float rho, const float (&U)[3], float we, float dpdx,
                                              const float (&N2)[3][3], const float (&R2)[3][3]);

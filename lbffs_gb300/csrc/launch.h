@@ -26,8 +26,8 @@ cudaError_t launch_q27(const StepArgs& a, const StepConfig& c, bool bulk, cudaSt
 cudaError_t setup_pack_bc(const int* boundary, const int* b1, const int* b2, const int* b3, uint16_t* bc, int nx,
                           int ny, int nz, cudaStream_t st);
 cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
-                           const float* omega, float omega0, float cs, int damping, uint8_t* flags, uint8_t* scratch,
-                           int nx, int ny, int nz, cudaStream_t st);
+                           const float* omega, float omega0, float cs, int damping, bool xface_special, uint8_t* flags,
+                           uint8_t* scratch, int nx, int ny, int nz, cudaStream_t st);
 // compaction of the fluid cells whose flags intersect mask (FL_SPECIAL: the boundary-kernel list):
 // counts[nblocks] per chunk of SETUP_CHUNK cells, then scatter
 constexpr int SETUP_CHUNK = 256;
@@ -48,6 +48,11 @@ cudaError_t halo_fill(int Q, int tsize, void* f, const uint8_t* flags, const uin
 cudaError_t fill_f32(float* p, float v, long long n, cudaStream_t st);
 // out[0] bit 0: a WallFunction code present, bit 1: an invalid code present (out[1]: the largest)
 cudaError_t setup_check_codes(const int* b1, const int* b2, const int* b3, long long E, int* out, cudaStream_t st);
+// *bad |= 1 unless every face carries one boundary code per axis (codes: code of axis d on the low /
+// high face s in bits 3 (2 d + s)) and the face flag (boundary) is set on exactly the border cells:
+// the condition under which the step kernels can pull across the border without a ghost layer
+cudaError_t setup_check_faces(const int* boundary, const int* b1, const int* b2, const int* b3, int codes, int nx,
+                              int ny, int nz, int* bad, cudaStream_t st);
 // counts[4] (zeroed by the caller): fluid, special, STL-link and macroscopic-storing cells
 cudaError_t setup_count_flags(const uint8_t* flags, long long E, unsigned long long* counts, cudaStream_t st);
 // FP64 partial sums: force over the listed cells (3 per block), mass over fluid cells (1 per block)

@@ -370,7 +370,25 @@ static int commit(lbffs_ctx* c)
             const int bit = 2 * (b - 1) + s;
             if (v == BC_OUTLET || v == BC_FIXDEN) c->sponge_mask |= (1 << bit);
             else c->sponge_mask &= ~(1 << bit);
+            c->face_codes = (c->face_codes & ~(7 << (3 * bit))) | ((v & 7) << (3 * bit));
         }
+    }
+    // one boundary code per face and axis (the codes just read) and the face flag on exactly the
+    // border cells: the step kernels can then pull across the border without a ghost layer
+    {
+        int* bad = nullptr;
+        CK(ctx_alloc_bytes(c, (void**)&bad, sizeof(int)));
+        int h = 0;
+        cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+        if (e == cudaSuccess)
+            e = setup_check_faces(c->iarr[0], c->iarr[1], c->iarr[2], c->iarr[3], c->face_codes, nx, ny, nz, bad,
+                                  c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        ctx_free(c, bad);
+        CK(e);
+        c->face_ok = h == 0;
+        c->xface_special = LBFFS_BORDER_PULLS && c->face_ok && c->arena == nullptr;
     }
     // uniform relaxation rate: the value at the domain centre
     const long long centre = ((long long)(nz / 2) * ny + ny / 2) * nx + nx / 2;
@@ -381,7 +399,7 @@ static int commit(lbffs_ctx* c)
     uint8_t* scratch = nullptr;
     CK(ctx_alloc_bytes(c, (void**)&scratch, E));
     cudaError_t e = setup_classify(c->Q, c->bc, c->solid, c->nei, c->sdf, c->omega, c->omega0, c->d.cs,
-                                   c->d.damping, c->flags, scratch, nx, ny, nz, c->stream);
+                                   c->d.damping, c->xface_special, c->flags, scratch, nx, ny, nz, c->stream);
     cudaStreamSynchronize(c->stream);
     ctx_free(c, scratch);
     CK(e);
@@ -578,6 +596,8 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
     a.clim = p->clim;
     a.cs = c->d.cs;
     a.damping = c->d.damping;
+    a.border_pulls = 0;
+    a.face_codes = c->face_codes;
     a.sponge_mask = c->sponge_mask;
     a.sgs = c->d.sgs;
     a.wall = c->d.wall;
@@ -640,12 +660,18 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
         CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
     }
+    // pulls across the grid's border: straight from where the face streaming takes them when the faces
+    // allow it (xface_special: the x-face cells are boundary-kernel cells), nothing changes the
+    // produced populations after the step (no IBM forcing pass) and the bulk kernel is the per-thread
+    // one; otherwise from the ghost layer, filled before every step
+    const bool pulls = c->xface_special && c->n_markers <= 1 && c->bulk_kind == 0;
     for (int s = 0; s < nsteps; s++) {
         StepArgs a;
         ctx_step_args(c, p, c->fcur, c->mcur, a);
         a.store_all = (p->store_fields == 2) || (p->store_fields == 1 && s == nsteps - 1);
+        a.border_pulls = pulls ? 1 : 0;
         // ghost layer of this step's source populations: the face streaming of the six faces
-        {
+        if (!pulls) {
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (c->timing) {
                 e0 = get_event(c);

@@ -45,20 +45,32 @@ constexpr uint8_t FL_SDF = 8;      // near-wall damping factor < 1: read sdf
 constexpr uint8_t FL_OMEGA = 16;   // omega differs from the uniform omega0: read omega[]
 constexpr uint8_t FL_LINK = 32;    // has at least one STL link
 constexpr uint8_t FL_FACE = 64;    // on the domain border (face codes apply)
+constexpr uint8_t FL_XFACE = 128;  // special only as an x-face cell of a border-pull context (its neighbours
+                                   // need not store their macroscopics)
 
 // bulk kernel tiling: BULK_BX threads per block, BULK_V cells per thread (32 apart)
 constexpr int BULK_BX = 128;
 constexpr int BULK_V = 2;
-// cells per thread of the D3Q27 bulk kernel (a build-time tuning value).  One: 27 populations per
-// thread leave room for twice the resident warps of two cells (80 against 116 registers), which
-// measured 11-15 % faster on the 768x192x192 LES step and 1.5 % on the 256^3 cavity.
+// cells per thread of the D3Q27 cumulant and WALE bulk kernels (a build-time tuning value).  One:
+// 27 populations per thread leave room for twice the resident warps of two cells (80 against 116
+// registers), which measured 11-15 % faster on the 768x192x192 LES step and 1.5 % on the 256^3 cavity.
 #ifndef LBFFS_BULK_V27
 #define LBFFS_BULK_V27 1
 #endif
-template <int Q>
+// D3Q27 recursive regularised bulk cells with Smagorinsky (or no) SGS: two cells per thread with the
+// moment-form collision on packed FP32x2 pairs (1), or the generic one-cell path (0); build-time
+#ifndef LBFFS_BULK_PAIR27
+#define LBFFS_BULK_PAIR27 1
+#endif
+// the step kernels can pull across the grid's border themselves (StepArgs::border_pulls); 0 compiles
+// that choice out, and the library then fills the ghost layer before every step (a build-time choice)
+#ifndef LBFFS_BORDER_PULLS
+#define LBFFS_BORDER_PULLS 1
+#endif
+template <int Q, int COLL = 0, int SGS = 0>
 __host__ __device__ constexpr int bulk_v()
 {
-    return Q == 19 ? BULK_V : LBFFS_BULK_V27;
+    return Q == 19 ? BULK_V : (LBFFS_BULK_PAIR27 && COLL == 0 && SGS == 0) ? 2 : LBFFS_BULK_V27;
 }
 
 constexpr float FP16S_SCALE = 32768.0f;  // (f - w) * 2^15 keeps |f - w| < 2 in range, 1.9e-9 above subnormals
@@ -198,6 +210,12 @@ struct StepArgs {
     int nx, ny, nz;
     float omega0, dpdx, les, omega_b, spz, clim, cs;
     int damping;      // near-wall damping of the Smagorinsky eddy viscosity (enum lbffs_damping)
+    // pulls across the grid's border: 0, from the ghost layer filled before each step (k_halo); 1,
+    // straight from where the face streaming takes them (every face carries one boundary code per
+    // axis: face_codes holds code (axis d, low / high face s) in bits 3 (2 d + s) .. 3 (2 d + s) + 2;
+    // x-face cells are boundary-kernel cells, bulk cells cross only y / z faces)
+    int border_pulls;
+    int face_codes;
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity
     int store_all;    // store rho/u/v/w/tau for every fluid cell this step
     int bulk_kind;    // D3Q19 bulk kernel: 0 per-thread loads, 1 row-staged bulk copies (launch choice)

@@ -32,7 +32,7 @@ cudaError_t setup_pack_bc(const int* boundary, const int* b1, const int* b2, con
 // pass 1: solid / face / link / special bits
 template <int Q>
 __global__ void k_classify1(const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, uint8_t* flags, int nx,
-                            int ny, int nz)
+                            int ny, int nz, bool xface_special)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx) return;
@@ -67,6 +67,9 @@ __global__ void k_classify1(const uint16_t* bc, const uint8_t* solid, const uint
     if (face || border) fl |= FL_FACE;
     if (link) fl |= FL_LINK;
     if (link || complex_bc) fl |= FL_SPECIAL;
+    // a border-pull context hands its x-face cells to the boundary kernel: bulk rows then never pull
+    // across an x face
+    else if (xface_special && (i == 0 || i == nx - 1)) fl |= FL_SPECIAL | FL_XFACE;
     flags[ic] = fl;
 }
 
@@ -96,9 +99,9 @@ __global__ void k_classify2(const uint8_t* pass1, uint8_t* flags, const float* s
                 if (jj >= ny) jj -= ny;
                 if (kk < 0) kk += nz;
                 if (kk >= nz) kk -= nz;
-                near |= (pass1[((long long)kk * ny + jj) * nx + ii] & FL_SPECIAL) != 0;
+                near |= (pass1[((long long)kk * ny + jj) * nx + ii] & (FL_SPECIAL | FL_XFACE)) == FL_SPECIAL;
             }
-    fl &= (FL_SPECIAL | FL_LINK | FL_FACE);
+    fl &= (FL_SPECIAL | FL_LINK | FL_FACE | FL_XFACE);
     if (near) fl |= FL_STORE;
     const float s = sdf[ic];
     if (s != 10000.f && s > 0.f &&
@@ -109,12 +112,12 @@ __global__ void k_classify2(const uint8_t* pass1, uint8_t* flags, const float* s
 }
 
 cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
-                           const float* omega, float omega0, float cs, int damping, uint8_t* flags, uint8_t* scratch,
-                           int nx, int ny, int nz, cudaStream_t st)
+                           const float* omega, float omega0, float cs, int damping, bool xface_special, uint8_t* flags,
+                           uint8_t* scratch, int nx, int ny, int nz, cudaStream_t st)
 {
     const dim3 grid((nx + 127) / 128, ny, nz);
-    if (Q == 19) k_classify1<19><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
-    else k_classify1<27><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
+    if (Q == 19) k_classify1<19><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz, xface_special);
+    else k_classify1<27><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz, xface_special);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_classify2<<<grid, 128, 0, st>>>(scratch, flags, sdf, omega, omega0, cs, damping, nx, ny, nz);
@@ -352,6 +355,34 @@ __global__ void k_check_codes(const int* __restrict__ b1, const int* __restrict_
 cudaError_t setup_check_codes(const int* b1, const int* b2, const int* b3, long long E, int* out, cudaStream_t st)
 {
     k_check_codes<<<512, 256, 0, st>>>(b1, b2, b3, E, out);
+    return cudaGetLastError();
+}
+
+__global__ void k_check_faces(const int* __restrict__ boundary, const int* __restrict__ b1,
+                              const int* __restrict__ b2, const int* __restrict__ b3, int codes, int nx, int ny,
+                              int nz, int* bad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const long long ic = ((long long)k * ny + j) * nx + i;
+    const int x[3] = {i, j, k}, N[3] = {nx, ny, nz};
+    const int* b[3] = {b1, b2, b3};
+    const bool border = i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (nz > 1 && (k == 0 || k == nz - 1));
+    bool ok = boundary[ic] == (border ? 1 : 0);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int e = x[d] == 0 ? (codes >> (6 * d)) & 7 : x[d] == N[d] - 1 ? (codes >> (6 * d + 3)) & 7 : 0;
+        ok &= b[d][ic] == e;
+    }
+    if (!ok) atomicOr(bad, 1);
+}
+
+cudaError_t setup_check_faces(const int* boundary, const int* b1, const int* b2, const int* b3, int codes, int nx,
+                              int ny, int nz, int* bad, cudaStream_t st)
+{
+    const dim3 grid((nx + 127) / 128, ny, nz);
+    k_check_faces<<<grid, 128, 0, st>>>(boundary, b1, b2, b3, codes, nx, ny, nz, bad);
     return cudaGetLastError();
 }
 

@@ -22,7 +22,7 @@ cudaError_t LBFFS_NAME(LBFFS_Q, LBFFS_S, LBFFS_C, LBFFS_PART)(const StepArgs& a,
     const dim3 grid((unsigned)((a.n_special + SPECIAL_BS - 1) / SPECIAL_BS));
     k_special<LBFFS_Q, LBFFS_S, LBFFS_C><<<grid, SPECIAL_BS, 0, st>>>(a);
 #else
-    constexpr int V = bulk_v<LBFFS_Q>();
+    constexpr int V = bulk_v<LBFFS_Q, LBFFS_C, LBFFS_PART == 2 ? SGS_WALE : SGS_SMAG>();
     const dim3 grid((a.nx + BULK_BX * V - 1) / (BULK_BX * V), a.ny, a.nz);
 #if LBFFS_PART == 0
     k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_SMAG, false><<<grid, BULK_BX, 0, st>>>(a);

@@ -280,6 +280,99 @@ __device__ __forceinline__ int missing_dir(int q, const int (&b)[3])
     return out;
 }
 
+// ---- border pulls (StepArgs::border_pulls 1): the face streaming without a ghost layer ----
+// A cell on the grid's border pulls population q from outside the grid when P - c_q lies there.  The
+// reference's face streaming (upwindID_B + reflectOrMirrorQ, D3Q19 kernel.cl:114-575, D3Q27
+// kernel.cl:1133-1146) then takes P's own previous value of missing_dir(q) when a crossed face of P
+// carries a wall code, else the previous value of q of the periodically wrapped upwind cell.  In this
+// mode the cell reads that value where it lies instead of from a ghost layer filled before the step.
+// A cell's face codes come from face_codes (one code per face and axis, checked when the geometry is
+// committed); the face flag is set on every border cell (on the z faces only when nz > 1).
+__device__ __forceinline__ int face_code(const StepArgs& a, int d, int s) { return (a.face_codes >> (3 * (2 * d + s))) & 7; }
+
+// the code of axis d of a cell at coordinate xd: its face's code when the cell is on a face of that
+// axis (the low face when the axis is one cell long), else 0
+__device__ __forceinline__ int cell_code(const StepArgs& a, int xd, int Nd, int d)
+{
+    return xd == 0 ? face_code(a, d, 0) : xd == Nd - 1 ? face_code(a, d, 1) : 0;
+}
+
+// Where a border cell's pulls come from: its border flags, face flag and codes, and per axis the
+// padded-index shift to the periodic image (grid extent times the axis stride).
+struct BorderCell {
+    bool lo[3], hi[3];
+    bool face;
+    int b[3];
+    int wrap[3];
+};
+
+__device__ __forceinline__ BorderCell border_cell(const StepArgs& a, int i, int j, int k)
+{
+    BorderCell g;
+    const int x[3] = {i, j, k}, N[3] = {a.nx, a.ny, a.nz}, st[3] = {1, a.px, a.pxy};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        g.lo[d] = x[d] == 0;
+        g.hi[d] = x[d] == N[d] - 1;
+        g.b[d] = cell_code(a, x[d], N[d], d);
+        g.wrap[d] = N[d] * st[d];
+    }
+    g.face = i == 0 || i == a.nx - 1 || j == 0 || j == a.ny - 1 || (a.nz > 1 && (k == 0 || k == a.nz - 1));
+    return g;
+}
+
+// The border of a bulk row (j, k) in a border-pull context: bulk cells are never x-face cells there,
+// so only the y / z faces are crossed (row_crosses: the row lies on one of them).  The row's x flags
+// and x code are left clear, so every bulk cell of the row shares the mapping.
+__device__ __forceinline__ bool row_crosses(const StepArgs& a, int j, int k)
+{
+    return a.border_pulls && (j == 0 || j == a.ny - 1 || k == 0 || k == a.nz - 1);
+}
+__device__ __forceinline__ BorderCell row_border(const StepArgs& a, int j, int k)
+{
+    BorderCell g;
+    g.lo[0] = g.hi[0] = false;
+    g.b[0] = 0;
+    g.wrap[0] = a.nx;
+    g.lo[1] = j == 0;
+    g.hi[1] = j == a.ny - 1;
+    g.lo[2] = k == 0;
+    g.hi[2] = k == a.nz - 1;
+    g.b[1] = cell_code(a, j, a.ny, 1);
+    g.b[2] = cell_code(a, k, a.nz, 2);
+    g.wrap[1] = a.ny * a.px;
+    g.wrap[2] = a.nz * a.pxy;
+    g.face = j == 0 || j == a.ny - 1 || (a.nz > 1 && (k == 0 || k == a.nz - 1));
+    return g;
+}
+
+// the element index (in the population array a.f_in, planes pE apart) that population q of border
+// cell g at padded index ip pulls: the ghost position ip - c_q of plane q moved to the periodic image,
+// or the cell's own element of the missing direction.  Plane and offset are formed arithmetically.
+template <int Q>
+__device__ __forceinline__ long long border_pull(const StepArgs& a, const BorderCell& g, int q, int ip)
+{
+    const int c[3] = {lat_c(Q, q, 0), lat_c(Q, q, 1), lat_c(Q, q, 2)};
+    int shift = 0;
+    bool out = false, wall = false;
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        if (c[e] > 0 && g.lo[e]) {  // P - c_q below the low face
+            out = true;
+            shift += g.wrap[e];
+            wall |= is_wall_code(g.b[e]);
+        } else if (c[e] < 0 && g.hi[e]) {  // above the high face
+            out = true;
+            shift -= g.wrap[e];
+            wall |= is_wall_code(g.b[e]);
+        }
+    }
+    const long long pull = (long long)q * a.pE + (ip - (c[0] + c[1] * a.px + c[2] * a.pxy));
+    if (!out) return pull;
+    if (!(g.face && wall)) return pull + shift;
+    return (long long)missing_dir<Q>(q, g.b) * a.pE + ip;
+}
+
 // The collision of one bulk cell whose Q pulled populations are in ft (held form for D3Q19):
 // macroscopics, eddy viscosity, sponge, stores of the macroscopic fields that are read later, and
 // the collision in place.
@@ -393,13 +486,16 @@ __device__ __forceinline__ bool plain_pair(const StepArgs& a, const uint8_t (&fl
 // plain (the same for the whole warp, see plain_pair): both cells active, uniform omega, no wall
 // damping, no field stores and no sponge, so the per-lane part reduces to the relaxation rates;
 // it computes the same numbers as the general path.
-template <int S, bool LES>
-__device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], const uint8_t (&fl)[2],
+// Q = 27: the same with the D3Q27 moments and recursive regularised collision (collide_rr27p).
+template <int S, bool LES, int Q = 19>
+__device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[Q], const uint8_t (&fl)[2],
                                               const bool (&act)[2], const int (&ci)[2], const int (&cj)[2],
                                               const int (&ck)[2], const int (&ic)[2], bool plain = false)
 {
     constexpr int HS = Codec<S>::HS;
-    const Mom19T<F2> m = moments19<Codec<S>::DEV, HS>(ft);
+    Mom19T<F2> m;
+    if constexpr (Q == 19) m = moments19<Codec<S>::DEV, HS>(ft);
+    else m = moments27p<Codec<S>::DEV, HS>(ft);
     float irl[2], oml[2];
 #pragma unroll
     for (int v = 0; v < 2; v++) {
@@ -448,7 +544,8 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[19], c
         wel[c] = 1.f / (tau + tsl[c]);
     }
     const F2 U[3] = {u - hd, v, w};
-    collide_rr19m<HS>(ft, m, U, pk(wel[0], wel[1]), ir, a.omega_b, a.dpdx);
+    if constexpr (Q == 19) collide_rr19m<HS>(ft, m, U, pk(wel[0], wel[1]), ir, a.omega_b, a.dpdx);
+    else collide_rr27p<HS, !Codec<S>::DEV>(ft, m, U, pk(wel[0], wel[1]), ir, a.omega_b, a.dpdx);
 }
 
 // Two cells of one thread through bulk_collide2, then the stores of the active ones.
@@ -459,12 +556,23 @@ __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)
 {
     using T = typename Codec<S>::T;
     F2 ft[19];
+    if (row_crosses(a, cj[0], ck[0]) || row_crosses(a, cj[1], ck[1])) {
+        const BorderCell rb[2] = {row_border(a, cj[0], ck[0]), row_border(a, cj[1], ck[1])};
+        const T* f = static_cast<const T*>(a.f_in);
 #pragma unroll
-    for (int q = 0; q < 19; q++) {
-        const T* p = static_cast<const T*>(a.fin_s[q]);
-        const float x0 = act[0] ? Codec<S>::load_held(p + ip[0]) : 0.f;
-        const float x1 = act[1] ? Codec<S>::load_held(p + ip[1]) : 0.f;
-        ft[q] = pk(x0, x1);
+        for (int q = 0; q < 19; q++) {
+            const float x0 = act[0] ? Codec<S>::load_held(f + border_pull<19>(a, rb[0], q, ip[0])) : 0.f;
+            const float x1 = act[1] ? Codec<S>::load_held(f + border_pull<19>(a, rb[1], q, ip[1])) : 0.f;
+            ft[q] = pk(x0, x1);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 19; q++) {
+            const T* p = static_cast<const T*>(a.fin_s[q]);
+            const float x0 = act[0] ? Codec<S>::load_held(p + ip[0]) : 0.f;
+            const float x1 = act[1] ? Codec<S>::load_held(p + ip[1]) : 0.f;
+            ft[q] = pk(x0, x1);
+        }
     }
     bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
 #pragma unroll
@@ -535,17 +643,21 @@ __device__ __forceinline__ void st_hint_b32(void* p, uint32_t v, uint64_t pol)
 __device__ __forceinline__ float held_bits(__half, uint16_t b) { return __half2float(__ushort_as_half(b)); }
 __device__ __forceinline__ float held_bits(__nv_bfloat16, uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
 
-// the 19 pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol
-template <int S, bool HINT>
+// the Q pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol; BORDER:
+// the row crosses a y / z face (rb: its border, border pulls; both cells share its mapping, so the
+// pulls with c_x = 0 stay one aligned 32-bit word)
+template <int S, bool HINT, int Q = 19, bool BORDER = false>
 __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool any, [[maybe_unused]] uint64_t pol,
-                                              F2 (&ft)[19])
+                                              F2 (&ft)[Q], [[maybe_unused]] const BorderCell* rb = nullptr)
 {
     using T = typename Codec<S>::T;
     static_assert(sizeof(T) == 2, "2-byte storage");
 #pragma unroll
-    for (int q = 0; q < 19; q++) {
-        const T* p = static_cast<const T*>(a.fin_s[q]) + ip0;
-        if (lat_c(19, q, 0) == 0) {
+    for (int q = 0; q < Q; q++) {
+        const T* p;
+        if constexpr (BORDER) p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, *rb, q, ip0);
+        else p = static_cast<const T*>(a.fin_s[q]) + ip0;
+        if (lat_c(Q, q, 0) == 0) {
             uint32_t wd = 0u;
             if constexpr (HINT) wd = any ? ld_hint_b32(p, pol) : 0u;
             else wd = any ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
@@ -566,14 +678,14 @@ __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool a
 
 // the results of two adjacent cells at ip0: one packed 32-bit store per direction when both are
 // active, else each active cell's own element
-template <int S, bool HINT>
-__device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)[19], const bool (&act)[2], int ip0,
+template <int S, bool HINT, int Q = 19>
+__device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)[Q], const bool (&act)[2], int ip0,
                                                [[maybe_unused]] uint64_t pol)
 {
     using T = typename Codec<S>::T;
     if (act[0] && act[1]) {
 #pragma unroll
-        for (int q = 0; q < 19; q++) {
+        for (int q = 0; q < Q; q++) {
             T* p = static_cast<T*>(a.fout_q[q]) + ip0;
             const uint32_t wd = held_pack(T{}, lane0(ft[q]), lane1(ft[q]));
             if constexpr (HINT) st_hint_b32(p, wd, pol);
@@ -581,7 +693,7 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
         }
     } else {
 #pragma unroll
-        for (int q = 0; q < 19; q++) {
+        for (int q = 0; q < Q; q++) {
             T* p = static_cast<T*>(a.fout_q[q]) + ip0;
             if (act[0]) Codec<S>::store_held(p, lane0(ft[q]));
             if (act[1]) Codec<S>::store_held(p + 1, lane1(ft[q]));
@@ -599,7 +711,12 @@ __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (
                                               const int (&ic)[2], int ip0, bool plain = false)
 {
     F2 ft[19];
-    if (LBFFS_BULK_EVICT && a.l2_policy != 0) {
+    if (row_crosses(a, cj[0], ck[0])) {
+        const BorderCell rb = row_border(a, cj[0], ck[0]);
+        pair_adj_load<S, false, 19, true>(a, ip0, act[0] || act[1], 0, ft, &rb);
+        bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+        pair_adj_store<S, false>(a, ft, act, ip0, 0);
+    } else if (LBFFS_BULK_EVICT && a.l2_policy != 0) {
         const uint64_t pol = a.l2_policy == 1 ? l2_policy_evict_first() : l2_policy_evict_normal();
         pair_adj_load<S, true>(a, ip0, act[0] || act[1], pol, ft);
         bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
@@ -642,7 +759,7 @@ __device__ __forceinline__ void bulk_prefetch(const StepArgs& a)
 // The adjacent pair of a bulk_block lane with its pulls issued together with its flag loads
 // (one memory round trip before the collision instead of two): the pair's pulls are read whenever
 // its first cell is in the row, active or not (a solid cell's values are read and dropped).
-template <int S, bool LES>
+template <int S, bool LES, int Q = 19>
 __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, int j, int k, int row, int prow,
                                                     bool inrange = true)
 {
@@ -652,49 +769,63 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
     fl[1] = valid && i0 + 1 < a.nx ? __ldg(a.flags + row + i0 + 1) : FL_SOLID;
     const bool hint = LBFFS_BULK_EVICT && a.l2_policy != 0;
     [[maybe_unused]] uint64_t pol = 0;
-    F2 ft[19];
-    if (hint) {
+    F2 ft[Q];
+    if (row_crosses(a, j, k)) {
+        const BorderCell rb = row_border(a, j, k);
+        pair_adj_load<S, false, Q, true>(a, prow + i0, valid, 0, ft, &rb);
+    } else if (hint) {
         pol = a.l2_policy == 1 ? l2_policy_evict_first() : l2_policy_evict_normal();
-        pair_adj_load<S, true>(a, prow + i0, valid, pol, ft);
+        pair_adj_load<S, true, Q>(a, prow + i0, valid, pol, ft);
     } else {
-        pair_adj_load<S, false>(a, prow + i0, valid, 0, ft);
+        pair_adj_load<S, false, Q>(a, prow + i0, valid, 0, ft);
     }
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
     const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
     if (!(act[0] || act[1])) return;
     const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
     const int ic[2] = {row + i0, row + i0 + 1};
-    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
-    if (hint) pair_adj_store<S, true>(a, ft, act, prow + i0, pol);
-    else pair_adj_store<S, false>(a, ft, act, prow + i0, 0);
+    bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain);
+    if (hint) pair_adj_store<S, true, Q>(a, ft, act, prow + i0, pol);
+    else pair_adj_store<S, false, Q>(a, ft, act, prow + i0, 0);
 }
 
 // bulk_pair (cells i0 and i0 + 32) with the pulls issued together with the flag loads; a cell's
 // pulls are read whenever it is in the row, active or not
-template <int S, bool LES>
+template <int S, bool LES, int Q = 19>
 __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j, int k, int row, int prow)
 {
     using T = typename Codec<S>::T;
     const bool valid[2] = {i0 < a.nx, i0 + 32 < a.nx};
     uint8_t fl[2];
-    F2 ft[19];
+    F2 ft[Q];
 #pragma unroll
     for (int v = 0; v < 2; v++) fl[v] = valid[v] ? __ldg(a.flags + row + i0 + 32 * v) : FL_SOLID;
+    if (row_crosses(a, j, k)) {
+        const BorderCell rb = row_border(a, j, k);
 #pragma unroll
-    for (int q = 0; q < 19; q++) {
-        const T* p = static_cast<const T*>(a.fin_s[q]) + prow + i0;
-        const float x0 = valid[0] ? Codec<S>::load_held(p) : 0.f;
-        const float x1 = valid[1] ? Codec<S>::load_held(p + 32) : 0.f;
-        ft[q] = pk(x0, x1);
+        for (int q = 0; q < Q; q++) {
+            const T* p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb, q, prow + i0);
+            const float x0 = valid[0] ? Codec<S>::load_held(p) : 0.f;
+            const float x1 = valid[1] ? Codec<S>::load_held(p + 32) : 0.f;
+            ft[q] = pk(x0, x1);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const T* p = static_cast<const T*>(a.fin_s[q]) + prow + i0;
+            const float x0 = valid[0] ? Codec<S>::load_held(p) : 0.f;
+            const float x1 = valid[1] ? Codec<S>::load_held(p + 32) : 0.f;
+            ft[q] = pk(x0, x1);
+        }
     }
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
     const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
     if (!(act[0] || act[1])) return;
     const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
     const int ic[2] = {row + i0, row + i0 + 32};
-    bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+    bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain);
 #pragma unroll
-    for (int q = 0; q < 19; q++) {
+    for (int q = 0; q < Q; q++) {
         T* p = static_cast<T*>(a.fout_q[q]) + prow + i0;
         if (act[0]) Codec<S>::store_held(p, lane0(ft[q]));
         if (act[1]) Codec<S>::store_held(p + 32, lane1(ft[q]));
@@ -711,10 +842,13 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
 {
     using T = typename Codec<S>::T;
     constexpr bool HELD = (Q == 19);
-    constexpr int V = bulk_v<Q>();
+    constexpr int V = bulk_v<Q, COLL, SGS>();
     // 2-byte D3Q19 pair path: a lane owns two adjacent cells (bulk_pair_adj); otherwise cells
     // lane + 32 v
     constexpr bool ADJ = Q == 19 && SGS != SGS_WALE && V == 2 && S != ST_FP32 && LBFFS_BULK_ADJ;
+    // D3Q27 recursive regularised collision on cell pairs (packed FP32x2): adjacent cells for 2-byte
+    // storage, cells 32 apart for FP32
+    constexpr bool PAIR27 = Q == 27 && V == 2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int base = (xb * (BULK_BX / 32) + warp) * (32 * V);
     const int i0 = ADJ ? base + 2 * lane : base + lane;
@@ -722,6 +856,11 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     const int row = (k * a.ny + j) * a.nx;
     const int prow = pidx(a, 0, j, k);
     bulk_prefetch<Q, S, V>(a);
+    if constexpr (PAIR27) {
+        if constexpr (S != ST_FP32) bulk_pair_adj_eager<S, LES, 27>(a, base + 2 * lane, j, k, row, prow);
+        else bulk_pair_eager<S, LES, 27>(a, base + lane, j, k, row, prow);
+        return;
+    }
     if constexpr (ADJ && LBFFS_BULK_EAGER) {
         bulk_pair_adj_eager<S, LES>(a, i0, j, k, row, prow);
         return;
@@ -752,14 +891,24 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip, plain);
     } else {
         float ft[V][Q];
+        const bool cross = row_crosses(a, j, k);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             if (!act[v]) continue;
             const int ip = prow + i0 + DV * v;
+            if (cross) {
+                const BorderCell rb = row_border(a, j, k);
 #pragma unroll
-            for (int q = 0; q < Q; q++) {
-                const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
-                ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+                for (int q = 0; q < Q; q++) {
+                    const T* p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb, q, ip);
+                    ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < Q; q++) {
+                    const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
+                    ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+                }
             }
         }
 #pragma unroll
@@ -825,10 +974,19 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
         for (int v = 0; v < BULK_V; v++) {
             if (!act[v]) continue;
             const int ip = pidx(a, ci[v], cj[v], ck[v]);
+            if (row_crosses(a, cj[v], ck[v])) {
+                const BorderCell rb = row_border(a, cj[v], ck[v]);
 #pragma unroll
-            for (int q = 0; q < Q; q++) {
-                const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
-                ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+                for (int q = 0; q < Q; q++) {
+                    const T* p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb, q, ip);
+                    ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < Q; q++) {
+                    const T* p = static_cast<const T*>(a.fin_s[q]) + ip;
+                    ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
+                }
             }
         }
 #pragma unroll
@@ -884,11 +1042,19 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
         return Codec<S>::load(static_cast<const T*>(a.fin_q[q]) + pcell, lat_w(Q, q));
     };
 
-    // streaming: upwind value, or the ghost that holds the face rule's value (upwindID_B +
-    // reflectOrMirrorQ, filled by k_halo)
+    // streaming: upwind value, or the face rule's value (upwindID_B + reflectOrMirrorQ): from the
+    // ghost that holds it (filled by k_halo), or, with border pulls, read where the rule takes it
     float ft[Q];
+    if (a.border_pulls && (x[0] == 0 || x[0] == N[0] - 1 || x[1] == 0 || x[1] == N[1] - 1 || x[2] == 0 ||
+                           x[2] == N[2] - 1)) {
+        const BorderCell g = border_cell(a, x[0], x[1], x[2]);
 #pragma unroll
-    for (int q = 0; q < Q; q++) ft[q] = Codec<S>::load(static_cast<const T*>(a.fin_s[q]) + ip, lat_w(Q, q));
+        for (int q = 0; q < Q; q++)
+            ft[q] = Codec<S>::load(static_cast<const T*>(a.f_in) + border_pull<Q>(a, g, q, ip), lat_w(Q, q));
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) ft[q] = Codec<S>::load(static_cast<const T*>(a.fin_s[q]) + ip, lat_w(Q, q));
+    }
 
     const float uo[3] = {a.u_p[ic], a.v_p[ic], a.w_p[ic]};
     const float omega_c = a.omega[ic];
