@@ -5,11 +5,12 @@ the OpenCL include block (ns.cpp:18-35) with the C-ABI headers and everything fr
 device section's ``try`` (ns.cpp:382) to the end of main() with ``ns_lbffs_block.inc``,
 writes the result to ``lbffs_gb300/driver/_dropin/<lattice>/ns.cpp`` and compiles it against
 ``liblbffs_cuda.so`` with the checkout's own headers on the include path.  The headers the
-driver includes and the cavity test case inputs are copied next to it (``inc/``,
-``cavity/``) so the same output can be compiled and run where the checkout is absent.
+driver includes and the inputs of two test cases are copied next to it (``inc/``, ``cavity/``,
+``cylinderIBM/``) so the same output can be compiled and run where the checkout is absent.
 Nothing of the checkout is committed; the output folder is git-ignored.
 
 usage: python lbffs_gb300/driver/make_dropin.py [--lbffs /path/to/LBFFS] [--no-compile]
+       (the checkout: --lbffs, else LBFFS_REFERENCE, else reference_dir()'s default)
 """
 from __future__ import annotations
 
@@ -21,6 +22,15 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 ROOT = os.path.dirname(PKG)
+
+
+def reference_dir() -> str:
+    """The LBFFS checkout this recipe reads: LBFFS_REFERENCE, else the build machine's checkout."""
+    return os.environ.get("LBFFS_REFERENCE", "/root/reference")
+
+
+def have_reference(lbffs: str = None) -> bool:
+    return os.path.isfile(os.path.join(lbffs or reference_dir(), "D3Q19_opencl", "ns.cpp"))
 
 
 def splice(ns_cpp: str) -> str:
@@ -46,10 +56,13 @@ def bundle(lbffs: str, lattice: str, out_dir: str) -> None:
         shutil.copy(os.path.join(lbffs, "src", f), inc)
     for f in BUNDLE_LAT:
         shutil.copy(os.path.join(lbffs, f"{lattice}_opencl", f.format(L=lattice)), inc)
-    case = os.path.join(out_dir, "cavity")
-    os.makedirs(case, exist_ok=True)
-    for f in ("input.txt", "boundaryConditions.txt"):
-        shutil.copy(os.path.join(lbffs, "testCases", "cavityFlow", f), case)
+    for name, src, files in (("cavity", "cavityFlow", ("input.txt", "boundaryConditions.txt")),
+                             ("cylinderIBM", "flowAroundCylinderIBM", ("input.txt", "boundaryConditions.txt",
+                                                                       "cylinder.stl"))):
+        case = os.path.join(out_dir, name)
+        os.makedirs(case, exist_ok=True)
+        for f in files:
+            shutil.copy(os.path.join(lbffs, "testCases", src, f), case)
 
 
 def compile_dropin(out_dir: str, lbffs: str = None, lattice: str = None) -> str:
@@ -84,7 +97,7 @@ def build(lbffs: str, lattice: str, compile_it: bool = True) -> str:
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--lbffs", default=os.environ.get("LBFFS_REFERENCE", "/root/reference"))
+    ap.add_argument("--lbffs", default=reference_dir())
     ap.add_argument("--no-compile", action="store_true")
     args = ap.parse_args(argv)
     for lat in ("D3Q19", "D3Q27"):

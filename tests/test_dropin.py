@@ -1,9 +1,12 @@
 """The drop-in: LBFFS's own driver (ns.cpp) with its OpenCL section replaced by the C ABI.
 
 CPU: the splice recipe produces a driver that compiles and links against liblbffs_cuda.so
-(needs the LBFFS checkout).  GPU: the spliced driver, compiled from its bundled headers,
-runs the reference's cavityFlow case inputs end to end (input parsing, boundary setup,
-initialisation, write.hpp output) and its restart file matches the CPU oracle.
+(needs the LBFFS checkout).  GPU: the spliced drivers, compiled from their bundled headers, run
+reduced versions of the reference's test cases end to end (input parsing, boundary setup,
+initialisation, moving-STL markers and motion, write.hpp output) and their restart files match the
+CPU oracle: cavityFlow on the D3Q19 driver, flowAroundCylinderIBM (cumulant, IBM) on the D3Q27
+driver.  The bundle is made by __graft_entry__.build() where the checkout is present and travels
+with the working tree; a GPU run without it fails rather than skips.
 """
 import os
 import subprocess
@@ -17,11 +20,18 @@ DROPIN = os.path.join(ROOT, "lbffs_gb300", "driver")
 sys.path.insert(0, DROPIN)
 import make_dropin  # noqa: E402
 
-REF = os.environ.get("LBFFS_REFERENCE", "/root/reference")
+REF = make_dropin.reference_dir()
+
+
+def _bundle(lattice, case):
+    out_dir = os.path.join(DROPIN, "_dropin", lattice)
+    if not os.path.exists(os.path.join(out_dir, "inc", "input.hpp")) or not os.path.isdir(os.path.join(out_dir, case)):
+        pytest.fail("drop-in bundle missing: run __graft_entry__.build() where the LBFFS checkout is present")
+    return out_dir
 
 
 def test_dropin_splices_and_compiles(cuda_lib):
-    if not os.path.isdir(os.path.join(REF, "D3Q19_opencl")):
+    if not make_dropin.have_reference(REF):
         pytest.skip("LBFFS checkout not present")
     for lat in ("D3Q19", "D3Q27"):
         exe = make_dropin.build(REF, lat)
@@ -36,9 +46,7 @@ def _set(lines, key, val):
 
 @pytest.mark.gpu
 def test_dropin_cavity_runs_on_gpu_and_matches_oracle(cuda_lib, oracle_built, tmp_path):
-    out_dir = os.path.join(DROPIN, "_dropin", "D3Q19")
-    if not os.path.exists(os.path.join(out_dir, "inc", "input.hpp")):
-        pytest.skip("drop-in bundle not generated (needs the LBFFS checkout where it is built)")
+    out_dir = _bundle("D3Q19", "cavity")
     exe = make_dropin.compile_dropin(out_dir)
     n, steps = 32, 200
     lines = open(os.path.join(out_dir, "cavity", "input.txt")).read().splitlines()
@@ -70,6 +78,61 @@ def test_dropin_cavity_runs_on_gpu_and_matches_oracle(cuda_lib, oracle_built, tm
              "nzMin": K.FaceBC(), "nzMax": K.FaceBC()}
     cs = K.make_case(n, n, 1, 19, faces, nu=float(nu), rho0=float(kv["rho0"]))
     o = R.OracleSolver(cs, sgs="wale", wall="bb", real="f32")
+    o.step(steps)
+    err = float(np.abs(f_gpu - o.f).max() / np.abs(o.f).max())
+    assert err < 1e-5, err
+
+
+@pytest.mark.gpu
+def test_dropin_d3q27_ibm_cylinder_runs_on_gpu_and_matches_oracle(cuda_lib, oracle_built, tmp_path):
+    """flowAroundCylinderIBM at 240x80x1 for 60 steps on the D3Q27 driver (its live selections: cumulant
+    collision, interpolated bounce-back, WALE): the rotating cylinder's markers are the facet centroids
+    of movingWalls.stl (stl.hpp setSTLc after normalizeSTLv) and its motion comes from input.txt
+    (walls.hpp readMotions).  The oracle runs the same case from the host mirror with the markers and
+    motion restated here; populations within 1e-5 relative."""
+    import re
+    out_dir = _bundle("D3Q27", "cylinderIBM")
+    exe = make_dropin.compile_dropin(out_dir)
+    nx, ny, steps = 240, 80, 60
+    src = os.path.join(out_dir, "cylinderIBM")
+    lines = open(os.path.join(src, "input.txt")).read().splitlines()
+    for k, v in (("nx", nx), ("ny", ny), ("nz", 1), ("endTimeStep", steps), ("outInterval", 30),
+                 ("writeBinary", "true"), ("Fwrite", "true"), ("restart", "false")):
+        lines = _set(lines, k, v)
+    (tmp_path / "input.txt").write_text("\n".join(lines) + "\n")
+    (tmp_path / "boundaryConditions.txt").write_text(open(os.path.join(src, "boundaryConditions.txt")).read())
+    stl = open(os.path.join(src, "cylinder.stl")).read()
+    (tmp_path / "movingWalls.stl").write_text(stl)
+    (tmp_path / "out").mkdir()
+    r = subprocess.run([exe], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "GB300 CUDA step: D3Q27" in r.stdout
+    raw = open(tmp_path / "out" / "data.dat", "rb").read()
+    assert list(np.frombuffer(raw[:16], dtype=np.int32)) == [steps, nx, ny, 1]
+    f_gpu = np.frombuffer(raw[16:], dtype=np.float32)
+
+    from lbffs_gb300 import case as K
+    from oracle import ref as R
+    kv = {ln.split()[0]: ln.split()[1].rstrip("f") for ln in lines if len(ln.split()) >= 2}
+    f32 = np.float32
+    L = f32(kv["Lx"]) / f32(nx - 1)
+    c = f32(kv["uMax"]) / f32(kv["U0"])
+    nu = f32(f32(kv["nu"]) / f32(L * c))
+    u_in = f32(1.0) / c
+    faces = {"nxMin": K.FaceBC(K.FIXEDVELOCITY, 0, 0, u_in, 0, 0), "nxMax": K.FaceBC(K.FIXEDDENSITY, 0, 0),
+             "nyMin": K.FaceBC(0, K.BOUNCEBACK, 0, u_in, 0, 0), "nyMax": K.FaceBC(0, K.BOUNCEBACK, 0, u_in, 0, 0),
+             "nzMin": K.FaceBC(), "nzMax": K.FaceBC()}
+    cs = K.make_case(nx, ny, 1, 27, faces, nu=float(nu), rho0=float(kv["rho0"]))
+    # markers: facet centroids of the vertices divided by L, in float (stl.hpp:161-185)
+    v = np.array(re.findall(r"vertex\s+(\S+)\s+(\S+)\s+(\S+)", stl), dtype=np.float32).reshape(-1, 3, 3) / L
+    markers = ((v[:, 0] + v[:, 1]) + v[:, 2]) / f32(3.0)
+    # walls.hpp:606-626: translations / c, rotOmega [rpm] * 2 pi / 60 / (c / L), centre / L
+    rot_omega = f32(float(f32(kv["rotOmega"]) * f32(2.0)) * np.pi / float(f32(60.0)) / float(c / L))
+    o = R.OracleSolver(cs, sgs="wale", wall="ibb", collision="cumulant", real="f32")
+    o.set_ibm(markers, float(f32(kv["uMovingTrans"]) / c), float(f32(kv["vMovingTrans"]) / c),
+              float(f32(kv["wMovingTrans"]) / c),
+              rot=(float(f32(kv["rotX"]) / L), float(f32(kv["rotY"]) / L), float(f32(kv["rotZ"]) / L)),
+              axis=(float(kv["rotAxisX"]), float(kv["rotAxisY"]), float(kv["rotAxisZ"])), rot_omega=float(rot_omega))
     o.step(steps)
     err = float(np.abs(f_gpu - o.f).max() / np.abs(o.f).max())
     assert err < 1e-5, err
