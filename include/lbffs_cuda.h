@@ -329,9 +329,13 @@ const char* lbffs_server_error(lbffs_server* srv, long long id);
    (a serving loop holding a fixed HBM budget, a driver that owns its own buffers and has no
    context): it calls no allocating routine and uses a fixed 256 KiB scratch array that every GPU
    loading this library keeps until exit.  The first call on a device looks up that array (and may
-   load the library's device code there); make it before any stream capture.  n_cells above
-   LBFFS_NOALLOC_MAX_CELLS is rejected with LBFFS_E_ARG.  Calls share the scratch: calls whose
-   kernels overlap on the GPU race.  Errors are reported by lbffs_last_error(NULL). */
+   load the library's device code there); make it before any stream capture.  That address is kept
+   per device for the life of the process, so the device's primary context must not be reset
+   (cudaDeviceReset) between calls.  n_cells above LBFFS_NOALLOC_MAX_CELLS, q other than 19 or 27,
+   null pointers and device ordinals of 64 or more are rejected with LBFFS_E_ARG before anything is
+   launched.  The caller's current device is the same after the call as before it.  Calls share
+   the scratch: calls whose kernels overlap on the GPU race.  Errors are reported by
+   lbffs_last_error(NULL). */
 #define LBFFS_NOALLOC_MAX_CELLS 268435456
 int lbffs_mass_noalloc(int device, const float* f, const unsigned char* solid, int q, long long n_cells,
                        double* out, void* stream);

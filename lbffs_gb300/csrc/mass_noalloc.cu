@@ -93,6 +93,25 @@ int na_fail(int code, const std::string& msg)
     return code;
 }
 
+// makes `device` current for the call and gives the caller's current device back on every return
+struct DeviceScope {
+    int saved = -1;
+    cudaError_t enter(int device)
+    {
+        cudaError_t e = cudaGetDevice(&saved);
+        if (e != cudaSuccess) {
+            saved = -1;
+            return e;
+        }
+        return saved == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceScope()
+    {
+        int cur = -1;
+        if (saved >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != saved) cudaSetDevice(saved);
+    }
+};
+
 }  // namespace
 
 extern "C" int lbffs_mass_noalloc(int device, const float* f, const unsigned char* solid, int q, long long n_cells,
@@ -109,7 +128,8 @@ extern "C" int lbffs_mass_noalloc(int device, const float* f, const unsigned cha
     if (device < 0 || device >= NA_MAX_DEVICES)
         return na_fail(LBFFS_E_ARG, "lbffs_mass_noalloc: device ordinal out of range");
 
-    cudaError_t e = cudaSetDevice(device);
+    DeviceScope scope;
+    cudaError_t e = scope.enter(device);
     if (e != cudaSuccess) return na_fail(LBFFS_E_CUDA, std::string("lbffs_mass_noalloc: cudaSetDevice: ") +
                                                            cudaGetErrorString(e));
     double* partials;

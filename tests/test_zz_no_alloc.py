@@ -83,3 +83,24 @@ def test_noalloc_mass_rejects_oversize(cuda_lib):
     assert b"exceeds the maximum" in cuda_lib.lbffs_last_error(None)
     torch.cuda.synchronize()
     assert out.item() == 7.0  # nothing was launched
+
+
+def test_noalloc_mass_empty_and_bad_arguments(cuda_lib):
+    """n_cells = 0 writes 0.0; q other than 19 / 27 and null pointers are refused with LBFFS_E_ARG and
+    leave the output untouched."""
+    import torch
+    fn = _bind(cuda_lib)
+    f_d = torch.ones(27 * 8, dtype=torch.float32, device="cuda:0")
+    s_d = torch.zeros(8, dtype=torch.uint8, device="cuda:0")
+    out = torch.full((1,), 7.0, dtype=torch.float64, device="cuda:0")
+    stream = torch.cuda.current_stream(0)
+    assert fn(0, f_d.data_ptr(), s_d.data_ptr(), 19, 0, out.data_ptr(), stream.cuda_stream) == 0
+    stream.synchronize()
+    assert out.item() == 0.0
+    out.fill_(7.0)
+    torch.cuda.synchronize()
+    assert fn(0, f_d.data_ptr(), s_d.data_ptr(), 20, 8, out.data_ptr(), None) == -1
+    assert fn(0, None, s_d.data_ptr(), 19, 8, out.data_ptr(), None) == -1
+    assert fn(0, f_d.data_ptr(), s_d.data_ptr(), 19, 8, None, None) == -1
+    torch.cuda.synchronize()
+    assert out.item() == 7.0
