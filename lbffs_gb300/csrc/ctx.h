@@ -43,12 +43,13 @@ struct lbffs_ctx {
     int sponge_mask = 0;
     bool dirty = true;
     // pulls across the grid's border: face_ok when every face carries one boundary code per axis
-    // (face_codes, StepArgs layout) and the face flag is set on exactly the border cells; a
-    // single-lattice context can then run without a ghost layer (xface_special: its x-face cells join
-    // the boundary kernel's list when the geometry is committed)
+    // (face_codes, StepArgs layout) and the face flag is set on exactly the border cells; pull_ok
+    // when moreover both x faces carry boundary-kernel codes (inlet / outlet / fixed density / wall
+    // function), so bulk rows cross only y / z faces: a single-lattice context then runs without a
+    // ghost layer
     int face_codes = 0;
     bool face_ok = false;
-    bool xface_special = false;
+    bool pull_ok = false;
     int* d_err = nullptr;
     float* stage = nullptr;
     size_t stage_elems = 0;

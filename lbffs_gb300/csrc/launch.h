@@ -26,8 +26,8 @@ cudaError_t launch_q27(const StepArgs& a, const StepConfig& c, bool bulk, cudaSt
 cudaError_t setup_pack_bc(const int* boundary, const int* b1, const int* b2, const int* b3, uint16_t* bc, int nx,
                           int ny, int nz, cudaStream_t st);
 cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
-                           const float* omega, float omega0, float cs, int damping, bool xface_special, uint8_t* flags,
-                           uint8_t* scratch, int nx, int ny, int nz, cudaStream_t st);
+                           const float* omega, float omega0, float cs, int damping, uint8_t* flags, uint8_t* scratch,
+                           int nx, int ny, int nz, cudaStream_t st);
 // compaction of the fluid cells whose flags intersect mask (FL_SPECIAL: the boundary-kernel list):
 // counts[nblocks] per chunk of SETUP_CHUNK cells, then scatter
 constexpr int SETUP_CHUNK = 256;

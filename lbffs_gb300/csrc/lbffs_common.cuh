@@ -45,8 +45,6 @@ constexpr uint8_t FL_SDF = 8;      // near-wall damping factor < 1: read sdf
 constexpr uint8_t FL_OMEGA = 16;   // omega differs from the uniform omega0: read omega[]
 constexpr uint8_t FL_LINK = 32;    // has at least one STL link
 constexpr uint8_t FL_FACE = 64;    // on the domain border (face codes apply)
-constexpr uint8_t FL_XFACE = 128;  // special only as an x-face cell of a border-pull context (its neighbours
-                                   // need not store their macroscopics)
 
 // bulk kernel tiling: BULK_BX threads per block, BULK_V cells per thread (32 apart)
 constexpr int BULK_BX = 128;
@@ -213,7 +211,7 @@ struct StepArgs {
     // pulls across the grid's border: 0, from the ghost layer filled before each step (k_halo); 1,
     // straight from where the face streaming takes them (every face carries one boundary code per
     // axis: face_codes holds code (axis d, low / high face s) in bits 3 (2 d + s) .. 3 (2 d + s) + 2;
-    // x-face cells are boundary-kernel cells, bulk cells cross only y / z faces)
+    // both x faces carry boundary-kernel codes, so bulk cells cross only y / z faces)
     int border_pulls;
     int face_codes;
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity

@@ -32,7 +32,7 @@ cudaError_t setup_pack_bc(const int* boundary, const int* b1, const int* b2, con
 // pass 1: solid / face / link / special bits
 template <int Q>
 __global__ void k_classify1(const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, uint8_t* flags, int nx,
-                            int ny, int nz, bool xface_special)
+                            int ny, int nz)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx) return;
@@ -67,9 +67,6 @@ __global__ void k_classify1(const uint16_t* bc, const uint8_t* solid, const uint
     if (face || border) fl |= FL_FACE;
     if (link) fl |= FL_LINK;
     if (link || complex_bc) fl |= FL_SPECIAL;
-    // a border-pull context hands its x-face cells to the boundary kernel: bulk rows then never pull
-    // across an x face
-    else if (xface_special && (i == 0 || i == nx - 1)) fl |= FL_SPECIAL | FL_XFACE;
     flags[ic] = fl;
 }
 
@@ -99,9 +96,9 @@ __global__ void k_classify2(const uint8_t* pass1, uint8_t* flags, const float* s
                 if (jj >= ny) jj -= ny;
                 if (kk < 0) kk += nz;
                 if (kk >= nz) kk -= nz;
-                near |= (pass1[((long long)kk * ny + jj) * nx + ii] & (FL_SPECIAL | FL_XFACE)) == FL_SPECIAL;
+                near |= (pass1[((long long)kk * ny + jj) * nx + ii] & FL_SPECIAL) != 0;
             }
-    fl &= (FL_SPECIAL | FL_LINK | FL_FACE | FL_XFACE);
+    fl &= (FL_SPECIAL | FL_LINK | FL_FACE);
     if (near) fl |= FL_STORE;
     const float s = sdf[ic];
     if (s != 10000.f && s > 0.f &&
@@ -112,12 +109,12 @@ __global__ void k_classify2(const uint8_t* pass1, uint8_t* flags, const float* s
 }
 
 cudaError_t setup_classify(int Q, const uint16_t* bc, const uint8_t* solid, const uint8_t* nei, const float* sdf,
-                           const float* omega, float omega0, float cs, int damping, bool xface_special, uint8_t* flags,
-                           uint8_t* scratch, int nx, int ny, int nz, cudaStream_t st)
+                           const float* omega, float omega0, float cs, int damping, uint8_t* flags, uint8_t* scratch,
+                           int nx, int ny, int nz, cudaStream_t st)
 {
     const dim3 grid((nx + 127) / 128, ny, nz);
-    if (Q == 19) k_classify1<19><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz, xface_special);
-    else k_classify1<27><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz, xface_special);
+    if (Q == 19) k_classify1<19><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
+    else k_classify1<27><<<grid, 128, 0, st>>>(bc, solid, nei, scratch, nx, ny, nz);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_classify2<<<grid, 128, 0, st>>>(scratch, flags, sdf, omega, omega0, cs, damping, nx, ny, nz);

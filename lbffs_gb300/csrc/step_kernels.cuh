@@ -998,13 +998,15 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
     }
 }
 
-// Resident CTAs per SM the D3Q19 bulk kernel may be compiled for (register budget 65536 / (128 x
-// this)); a build-time tuning value.  Left undefined, the register count is the compiler's choice.
-#ifdef LBFFS_BULK_MINB19
-#define LBFFS_BULK_BOUNDS(Q) __launch_bounds__(BULK_BX, (Q) == 19 ? LBFFS_BULK_MINB19 : 1)
-#else
-#define LBFFS_BULK_BOUNDS(Q) __launch_bounds__(BULK_BX)
+// Resident CTAs per SM the D3Q19 / D3Q27 bulk kernels may be compiled for (register budget 65536 /
+// (128 x this)); build-time tuning values.  1 leaves the register count to the compiler.
+#ifndef LBFFS_BULK_MINB19
+#define LBFFS_BULK_MINB19 1
 #endif
+#ifndef LBFFS_BULK_MINB27
+#define LBFFS_BULK_MINB27 1
+#endif
+#define LBFFS_BULK_BOUNDS(Q) __launch_bounds__(BULK_BX, (Q) == 19 ? LBFFS_BULK_MINB19 : LBFFS_BULK_MINB27)
 
 template <int Q, int S, int COLL, int SGS, bool LES>
 __global__ void LBFFS_BULK_BOUNDS(Q) k_bulk(const StepArgs a)
