@@ -116,6 +116,9 @@ def make_workload(name):
         n = 128
         c = K.make_case(n, n, n, 27, K.cavity_faces(0.05), nu=0.032)
         return c, dict(collision="rr", sgs="smag", wall="ibb", les=0.0)
+    if name == "cavity256x64_q27":
+        c = K.make_case(256, 256, 64, 27, K.cavity_faces(0.05), nu=0.032)
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=0.0)
     if name == "cavity256_q27":
         n = 256
         c = K.make_case(n, n, n, 27, K.cavity_faces(0.05), nu=0.032)
@@ -139,6 +142,15 @@ def make_workload(name):
         c.u0[inlet] *= (1.0 + rng.uniform(-0.01, 0.01, int(inlet.sum()))).astype(np.float32)
         c.f = None
         return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=64.0 / nx, rest=True)
+    if name == "step384_q27":
+        # the backward-facing step at half size in each direction (profiling size, populations larger
+        # than L2): the same boundaries, LES, damping and sponge as the 768x192x192 case
+        nx, ny, nz, h = 384, 96, 96, 32
+        solid, sdf = G.backward_step(nx, ny, nz, 64, h)
+        c = K.make_case(nx, ny, nz, 27, K.channel_faces(0.06, top_bottom=K.BOUNCEBACK, z_periodic=True),
+                        nu=0.06 * h / 5500.0, solid=solid, sdf=sdf)
+        c.f = None
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=32.0 / nx, rest=True)
     if name == "bluff1024_q27":
         # bluff body from a seeded procedural STL: a closed ellipsoid mesh of 20,000 triangles with
         # 5 % radial noise, 400 cells long, in a 1024x384x384 D3Q27 channel (inlet 0.05, Geier outlet,
@@ -285,9 +297,13 @@ def describe(name, storage):
                             "the 256-cell rows of the 256^3 case, populations larger than L2)",
             "cavity256_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256^3 (synthetic)",
             "cavity128_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 128^3 (synthetic, profiling size)",
+            "cavity256x64_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256x256x64 (synthetic, profiling size: "
+                                "populations larger than L2)",
             "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)",
             "step768_q27": f"backward-facing step D3Q27 RR IBB LES {storage.upper()} 768x192x192, step 64, Re 5500, "
                            "sponge 64 cells (synthetic)",
+            "step384_q27": f"backward-facing step D3Q27 RR IBB LES {storage.upper()} 384x96x96, step 32 (synthetic, "
+                           "profiling size)",
             "bluff1024_q27": f"bluff body D3Q27 RR IBB LES {storage.upper()} 1024x384x384, 20,000-triangle noisy "
                              "ellipsoid (400 cells) voxelised on the device, IBM cylinder D=32 with 512 markers "
                              "(synthetic)"}[name]
