@@ -513,12 +513,39 @@ __device__ __forceinline__ bool plain_pair(const StepArgs& a, const uint8_t (&fl
            a.sponge_mask == 0;
 }
 
+// cell (i, j, k) lies in a sponge zone: the conditions of sponge_tau, which leaves tau unchanged
+// everywhere else
+__device__ __forceinline__ bool in_sponge(const StepArgs& a, int i, int j, int k)
+{
+    if (a.sponge_mask == 0) return false;
+    const int x[3] = {i, j, k};
+    const int N[3] = {a.nx, a.ny, a.nz};
+    bool s = false;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const float n = (float)N[d];
+        if ((a.sponge_mask >> (2 * d)) & 1) s |= (float)x[d] < n * a.spz;
+        if ((a.sponge_mask >> (2 * d + 1)) & 1) s |= (float)x[d] > n * (1.f - a.spz);
+    }
+    return s;
+}
+
+// plain_pair for the cells (i0, j, k) and (i1, j, k): a sponge zone elsewhere in the lattice does not
+// take them off the plain path
+__device__ __forceinline__ bool plain_pair(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2], int i0,
+                                           int i1, int j, int k)
+{
+    return act[0] && act[1] && !((fl[0] | fl[1]) & (FL_OMEGA | FL_SDF | FL_STORE)) && !a.store_all && !a.ibm_box &&
+           !in_sponge(a, i0, j, k) && !in_sponge(a, i1, j, k);
+}
+
 // bulk_collide for the two cells of a thread at once (D3Q19, Smagorinsky or no SGS): the moments,
 // the velocity and the recursive regularised collision run on packed FP32x2 lanes (lane v = cell
 // v); the per-cell parts (relaxation rates, eddy viscosity square roots, sponge, field stores)
 // run per lane.  act[v]: cell v is a bulk cell (the other lane's values are computed and dropped).
 // plain (the same for the whole warp, see plain_pair): both cells active, uniform omega, no wall
-// damping, no field stores and no sponge, so the per-lane part reduces to the relaxation rates;
+// damping, no field stores and outside the sponge zones, so the per-lane part reduces to the
+// relaxation rates;
 // it computes the same numbers as the general path.
 // Q = 27: the same with the D3Q27 moments and recursive regularised collision (collide_rr27p).
 template <int S, bool LES, int Q = 19>
@@ -824,7 +851,7 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
         if (i0 + 1 == a.nx - 1) xface_fix<S, Q, 1>(a, i0 + 1, j, k, prow + i0 + 1, ft);
     }
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
-    const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
+    const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act, i0, i0 + 1, j, k));
     if (!(act[0] || act[1])) return;
     const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
     const int ic[2] = {row + i0, row + i0 + 1};
@@ -867,7 +894,7 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
         if (valid[1] && i0 + 32 == a.nx - 1) xface_fix<S, Q, 1>(a, i0 + 32, j, k, prow + i0 + 32, ft);
     }
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
-    const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
+    const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act, i0, i0 + 32, j, k));
     if (!(act[0] || act[1])) return;
     const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
     const int ic[2] = {row + i0, row + i0 + 32};
