@@ -131,8 +131,8 @@ def make_workload(name):
         return c, dict(collision="rr", sgs="smag", wall="ibb", les=0.0)
     if name == "step768_q27":
         # backward-facing step: 768x192x192, step 64 high ending at x = 128, inlet 0.06 with a
-        # seeded +-1 % per-cell perturbation, Re 5500 on the step height, Smagorinsky LES with the
-        # near-wall damping, sponge over the last 64 cells before the Geier outlet
+        # seeded +-1 % per-cell perturbation, Re 5500 on the step height, Smagorinsky LES (Cs 0.1) with
+        # Van Driest wall damping, sponge over the last 64 cells before the Geier outlet
         nx, ny, nz, h = 768, 192, 192, 64
         solid, sdf = G.backward_step(nx, ny, nz, 128, h)
         c = K.make_case(nx, ny, nz, 27, K.channel_faces(0.06, top_bottom=K.BOUNCEBACK, z_periodic=True),
@@ -141,7 +141,7 @@ def make_workload(name):
         inlet = c.boundary1 == K.FIXEDVELOCITY
         c.u0[inlet] *= (1.0 + rng.uniform(-0.01, 0.01, int(inlet.sum()))).astype(np.float32)
         c.f = None
-        return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=64.0 / nx, rest=True)
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=64.0 / nx, rest=True, damping="vandriest")
     if name == "step384_q27":
         # the backward-facing step at half size in each direction (profiling size, populations larger
         # than L2): the same boundaries, LES, damping and sponge as the 768x192x192 case
@@ -150,7 +150,7 @@ def make_workload(name):
         c = K.make_case(nx, ny, nz, 27, K.channel_faces(0.06, top_bottom=K.BOUNCEBACK, z_periodic=True),
                         nu=0.06 * h / 5500.0, solid=solid, sdf=sdf)
         c.f = None
-        return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=32.0 / nx, rest=True)
+        return c, dict(collision="rr", sgs="smag", wall="ibb", les=1.0, spz=32.0 / nx, rest=True, damping="vandriest")
     if name == "bluff1024_q27":
         # bluff body from a seeded procedural STL: a closed ellipsoid mesh of 20,000 triangles with
         # 5 % radial noise, 400 cells long, in a 1024x384x384 D3Q27 channel (inlet 0.05, Geier outlet,
@@ -300,7 +300,8 @@ def describe(name, storage):
             "cavity256x64_q27": f"lid-driven cavity D3Q27 RR {storage.upper()} 256x256x64 (synthetic, profiling size: "
                                 "populations larger than L2)",
             "cylinder1024": f"cylinder channel D3Q19 RR IBB {storage.upper()} 1024x256x4, D=40, Re=100 (synthetic)",
-            "step768_q27": f"backward-facing step D3Q27 RR IBB LES {storage.upper()} 768x192x192, step 64, Re 5500, "
+            "step768_q27": f"backward-facing step D3Q27 RR IBB LES (Van Driest damping) {storage.upper()} 768x192x192, "
+                           "step 64, Re 5500, "
                            "sponge 64 cells (synthetic)",
             "step384_q27": f"backward-facing step D3Q27 RR IBB LES {storage.upper()} 384x96x96, step 32 (synthetic, "
                            "profiling size)",
@@ -317,7 +318,7 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
     import lbffs_gb300 as L
     c, sel = make_workload(name)
     lat = L.Lattice(c.nx, c.ny, c.nz, q=c.q, storage=storage, collision=sel["collision"], sgs=sel["sgs"],
-                    wall=sel["wall"], device=device)
+                    wall=sel["wall"], device=device, damping=sel.get("damping", "wall"))
     if c.q == 19:
         lat.set_bulk_kernel(BULK_KIND)
     if sel.get("rest"):
@@ -379,6 +380,23 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
         out["special_ms"] = sp_ms / max(nsp, 1)
         out["halo_ms"] = h_ms / max(nh, 1)
     return out
+
+
+def force_series(res, samples=20, every=250):
+    """Drag / lift coefficients of the cylinder channel over time from the FP64 wall-force sum
+    (lbffs_force_sum), normalised as D3Q19_opencl/write.hpp:104 in lattice units: F / (1/2 rho_av U^2 D nz)
+    with the inlet speed U = 0.05, the diameter D = 40 cells and the z extent nz (the frontal area)."""
+    lat, c = res["lat"], res["case"]
+    n_fluid = float((c.solid == 0).sum()) if c.solid is not None else float(c.elements)
+    scale = 1.0 / (0.5 * 0.05 ** 2 * 40.0 * c.nz)
+    out = []
+    for s in range(samples):
+        lat.step(every, store_fields=0)
+        fw = lat.force_sum()
+        rho_av = lat.mass() / n_fluid
+        out.append([(s + 1) * every, fw[0] * scale / rho_av, fw[1] * scale / rho_av])
+    return {"every_steps": every, "t_cx_cy": [[int(t), round(float(a), 6), round(float(b), 6)] for t, a, b in out],
+            "note": "after the timed steps, from the channel started at rest (start-up transient)"}
 
 
 def run_e2e(res, steps, device):
@@ -559,6 +577,8 @@ def main():
                     "bulk_GBps": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9,
                     "bulk_frac_of_peak": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9 / peak,
                     "bytes_per_cell": vb}
+                if vname == "cylinder1024":
+                    variants[f"{vname}_{vst}"]["force_coefficients"] = force_series(r)
                 if r["setup"]:
                     variants[f"{vname}_{vst}"]["setup"] = r["setup"]
                     variants[f"{vname}_{vst}"]["ibm_ms"] = r.get("ibm_ms")
