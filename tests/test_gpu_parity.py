@@ -162,6 +162,19 @@ def test_run_to_run_bitwise_deterministic(cuda_lib):
     assert np.array_equal(a.download("f"), b.download("f"))
 
 
+@pytest.mark.parametrize("name", ["ibm_q19", "bluff_q27_les_ibm"])
+def test_ibm_run_to_run_bitwise_deterministic(cuda_lib, name):
+    """The IBM spread adds each marker's float-valued weighted force into an FP64 accumulator with
+    atomics.  A double holds 53 significant bits and each float term 24, so the sum of one cell's terms
+    is exact, and independent of the order in which the markers arrive, as long as those terms span
+    fewer than 29 binary orders of magnitude, which they do on these cases."""
+    _, _, a = run_gpu(name)
+    _, _, b = run_gpu(name)
+    assert np.array_equal(a.download("f"), b.download("f"))
+    assert np.array_equal(a.markers(), b.markers())
+    assert np.array_equal(a.download("gx"), b.download("gx"))
+
+
 def test_fp64_mass_matches_oracle_and_is_conserved(cuda_lib, oracle_built):
     """FP64 mass reduction matches the FP64 oracle; over further steps the FP32 mass drift of the closed
     cavity stays within twice the FP32 oracle's own drift on the same case (the reference's FP32 path
