@@ -577,6 +577,10 @@ def main():
                     "bulk_GBps": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9,
                     "bulk_frac_of_peak": vb * vn / (r["bulk_ms"] * 1e-3) / 1e9 / peak,
                     "bytes_per_cell": vb}
+                if vst == "bf16s":
+                    variants[f"{vname}_{vst}"]["accuracy"] = (
+                        "below the 1e-3 velocity-error bar of reduced-precision storage (FP16S meets it); "
+                        "not an equal alternative to FP16S")
                 if vname == "cylinder1024":
                     variants[f"{vname}_{vst}"]["force_coefficients"] = force_series(r)
                 if r["setup"]:

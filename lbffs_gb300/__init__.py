@@ -131,7 +131,8 @@ def _ptr(a):
 class Lattice:
     """One device lattice: the C-ABI context plus host-side conveniences.
 
-    ``q`` 19 or 27; ``storage`` "fp32" | "fp16s" | "bf16s"; ``collision`` "rr" | "cumulant";
+    ``q`` 19 or 27; ``storage`` "fp32" | "fp16s" | "bf16s" (BF16S: below the 1e-3 velocity-error bar
+    that FP16S meets); ``collision`` "rr" | "cumulant";
     ``sgs`` "smag" | "wale"; ``wall`` "bb" | "ibb"; ``damping`` (near-wall damping of the Smagorinsky
     eddy viscosity) "wall" (the reference's live factor) | "vandriest" | "none".
     """

@@ -44,7 +44,8 @@ struct lbffs_ctx {
     bool dirty = true;
     // pulls across the grid's border: face_ok when every face carries one boundary code per axis
     // (face_codes, StepArgs layout) and the face flag is set on exactly the border cells; pull_ok
-    // when moreover the context is a single lattice (not a server case): it then runs without a
+    // when moreover both x faces carry boundary-kernel codes (inlet / outlet / fixed density / wall
+    // function), so bulk rows cross only y / z faces: a single-lattice context then runs without a
     // ghost layer
     int face_codes = 0;
     bool face_ok = false;

@@ -388,7 +388,13 @@ static int commit(lbffs_ctx* c)
         ctx_free(c, bad);
         CK(e);
         c->face_ok = h == 0;
-        c->pull_ok = LBFFS_BORDER_PULLS && c->face_ok && c->arena == nullptr;
+        // the bulk kernels cross only y / z faces: both x faces must be boundary-kernel faces (x-face
+        // bulk cells reading across the x face measured slower than the ghost fill they save)
+        auto kernel_face = [](int code) {
+            return code == BC_OUTLET || code == BC_FIXVEL || code == BC_FIXDEN || code == BC_WALLFN;
+        };
+        c->pull_ok = LBFFS_BORDER_PULLS && c->face_ok && c->arena == nullptr && kernel_face(c->face_codes & 7) &&
+                     kernel_face((c->face_codes >> 3) & 7);
     }
     // uniform relaxation rate: the value at the domain centre
     const long long centre = ((long long)(nz / 2) * ny + ny / 2) * nx + nx / 2;
@@ -661,9 +667,9 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
         CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
     }
     // pulls across the grid's border: straight from where the face streaming takes them when the faces
-    // allow it (pull_ok), nothing changes the produced populations after the step (no IBM forcing
-    // pass) and the bulk kernel is the per-thread one; otherwise from the ghost layer, filled before
-    // every step
+    // allow it (pull_ok: the x-face cells are boundary-kernel cells), nothing changes the produced
+    // populations after the step (no IBM forcing pass) and the bulk kernel is the per-thread one;
+    // otherwise from the ghost layer, filled before every step
     const bool pulls = c->pull_ok && c->n_markers <= 1 && c->bulk_kind == 0;
     for (int s = 0; s < nsteps; s++) {
         StepArgs a;

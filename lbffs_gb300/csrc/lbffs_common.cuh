@@ -211,7 +211,7 @@ struct StepArgs {
     // pulls across the grid's border: 0, from the ghost layer filled before each step (k_halo); 1,
     // straight from where the face streaming takes them (every face carries one boundary code per
     // axis: face_codes holds code (axis d, low / high face s) in bits 3 (2 d + s) .. 3 (2 d + s) + 2;
-    // a bulk row crosses its y / z faces by the row's border, an x-face cell its x face by its own)
+    // both x faces carry boundary-kernel codes, so bulk cells cross only y / z faces)
     int border_pulls;
     int face_codes;
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity

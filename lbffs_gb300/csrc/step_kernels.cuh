@@ -321,9 +321,9 @@ __device__ __forceinline__ BorderCell border_cell(const StepArgs& a, int i, int 
     return g;
 }
 
-// The border of a bulk row (j, k) in a border-pull context: the y / z faces it crosses (row_crosses:
-// the row lies on one of them).  The row's x flags and x code are left clear, so every cell of the
-// row shares the mapping; an x-face cell then re-reads its pulls across the x face (xface_fix).
+// The border of a bulk row (j, k) in a border-pull context: bulk cells are never x-face cells there,
+// so only the y / z faces are crossed (row_crosses: the row lies on one of them).  The row's x flags
+// and x code are left clear, so every bulk cell of the row shares the mapping.
 __device__ __forceinline__ bool row_crosses(const StepArgs& a, int j, int k)
 {
     return a.border_pulls && (j == 0 || j == a.ny - 1 || k == 0 || k == a.nz - 1);
@@ -371,40 +371,6 @@ __device__ __forceinline__ long long border_pull(const StepArgs& a, const Border
     if (!out) return pull;
     if (!(g.face && wall)) return pull + shift;
     return (long long)missing_dir<Q>(q, g.b) * a.pE + ip;
-}
-
-// An x-face bulk cell (i = 0 or nx - 1) of a border-pull context: after its row's pulls, the pulls
-// that cross its x face (c_x = +1 on the low face, -1 on the high face) are read again with the
-// cell's own border.  Lane V of a pair (held values), or one cell's values (cell_fix).
-template <int S, int Q, int V>
-__device__ __forceinline__ void xface_fix(const StepArgs& a, int i, int j, int k, int ip, F2 (&ft)[Q])
-{
-    using T = typename Codec<S>::T;
-    const BorderCell g = border_cell(a, i, j, k);
-    const T* f = static_cast<const T*>(a.f_in);
-#pragma unroll
-    for (int q = 1; q < Q; q++) {
-        const int cx = lat_c(Q, q, 0);
-        if ((cx > 0 && g.lo[0]) || (cx < 0 && g.hi[0])) {
-            const float x = Codec<S>::load_held(f + border_pull<Q>(a, g, q, ip));
-            ft[q] = V == 0 ? pk(x, lane1(ft[q])) : pk(lane0(ft[q]), x);
-        }
-    }
-}
-template <int S, int Q, bool HELD>
-__device__ __forceinline__ void xface_fix_cell(const StepArgs& a, int i, int j, int k, int ip, float (&ft)[Q])
-{
-    using T = typename Codec<S>::T;
-    const BorderCell g = border_cell(a, i, j, k);
-    const T* f = static_cast<const T*>(a.f_in);
-#pragma unroll
-    for (int q = 1; q < Q; q++) {
-        const int cx = lat_c(Q, q, 0);
-        if ((cx > 0 && g.lo[0]) || (cx < 0 && g.hi[0])) {
-            const T* p = f + border_pull<Q>(a, g, q, ip);
-            ft[q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
-        }
-    }
 }
 
 // The collision of one bulk cell whose Q pulled populations are in ft (held form for D3Q19):
@@ -635,10 +601,6 @@ __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)
             ft[q] = pk(x0, x1);
         }
     }
-    if (a.border_pulls) {
-        if (act[0] && (ci[0] == 0 || ci[0] == a.nx - 1)) xface_fix<S, 19, 0>(a, ci[0], cj[0], ck[0], ip[0], ft);
-        if (act[1] && (ci[1] == 0 || ci[1] == a.nx - 1)) xface_fix<S, 19, 1>(a, ci[1], cj[1], ck[1], ip[1], ft);
-    }
     bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
 #pragma unroll
     for (int q = 0; q < 19; q++) {
@@ -776,11 +738,9 @@ __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (
                                               const int (&ic)[2], int ip0, bool plain = false)
 {
     F2 ft[19];
-    if (a.border_pulls && (row_crosses(a, cj[0], ck[0]) || ci[0] == 0 || ci[0] >= a.nx - 2)) {
+    if (row_crosses(a, cj[0], ck[0])) {
         const BorderCell rb = row_border(a, cj[0], ck[0]);
         pair_adj_load<S, false, 19, true>(a, ip0, act[0] || act[1], 0, ft, &rb);
-        if (act[0] && (ci[0] == 0 || ci[0] == a.nx - 1)) xface_fix<S, 19, 0>(a, ci[0], cj[0], ck[0], ip0, ft);
-        if (act[1] && ci[1] == a.nx - 1) xface_fix<S, 19, 1>(a, ci[1], cj[1], ck[1], ip0 + 1, ft);
         bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
         pair_adj_store<S, false>(a, ft, act, ip0, 0);
     } else if (LBFFS_BULK_EVICT && a.l2_policy != 0) {
@@ -846,10 +806,6 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
     } else {
         pair_adj_load<S, false, Q>(a, prow + i0, valid, 0, ft);
     }
-    if (a.border_pulls && valid) {
-        if (i0 == 0 || i0 == a.nx - 1) xface_fix<S, Q, 0>(a, i0, j, k, prow + i0, ft);
-        if (i0 + 1 == a.nx - 1) xface_fix<S, Q, 1>(a, i0 + 1, j, k, prow + i0 + 1, ft);
-    }
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
     const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act, i0, i0 + 1, j, k));
     if (!(act[0] || act[1])) return;
@@ -888,10 +844,6 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
             const float x1 = valid[1] ? Codec<S>::load_held(p + 32) : 0.f;
             ft[q] = pk(x0, x1);
         }
-    }
-    if (a.border_pulls) {
-        if (valid[0] && (i0 == 0 || i0 == a.nx - 1)) xface_fix<S, Q, 0>(a, i0, j, k, prow + i0, ft);
-        if (valid[1] && i0 + 32 == a.nx - 1) xface_fix<S, Q, 1>(a, i0 + 32, j, k, prow + i0 + 32, ft);
     }
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
     const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act, i0, i0 + 32, j, k));
@@ -985,8 +937,6 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
                     ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
                 }
             }
-            const int i = i0 + DV * v;
-            if (a.border_pulls && (i == 0 || i == a.nx - 1)) xface_fix_cell<S, Q, HELD>(a, i, j, k, ip, ft[v]);
         }
 #pragma unroll
         for (int v = 0; v < V; v++) {
@@ -1065,8 +1015,6 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
                     ft[v][q] = HELD ? Codec<S>::load_held(p) : Codec<S>::load(p, lat_w(Q, q));
                 }
             }
-            if (a.border_pulls && (ci[v] == 0 || ci[v] == a.nx - 1))
-                xface_fix_cell<S, Q, HELD>(a, ci[v], cj[v], ck[v], ip, ft[v]);
         }
 #pragma unroll
         for (int v = 0; v < BULK_V; v++) {

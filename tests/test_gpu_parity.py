@@ -122,8 +122,12 @@ def test_fp16s_velocity_error_vs_fp64_oracle(cuda_lib, oracle_built):
         _, _, lat = run_gpu(None, storage=st, steps=300, c=c, run=run)
         _, u, v, w = lat.macros()
         out[st] = float(np.linalg.norm(np.stack([u, v, w]) - ref) / np.linalg.norm(ref))
+    print("velocity error vs FP64 oracle, 24^3 cavity, 300 steps:", out)
     assert out["fp32"] < 1e-5, out
     assert out["fp16s"] < 1e-3, out
+    # BF16S (8 significand bits on f - w) does not meet the 1e-3 accuracy bar of the reduced-precision
+    # storage; it is kept as a storage option below that bar, and this bound only guards it from
+    # getting worse
     assert out["bf16s"] < 5e-2, out
 
 
