@@ -194,6 +194,14 @@ int lbffs_cell_counts(lbffs_ctx* ctx, long long out[4]);
    D3Q27 contexts always use kind 0. */
 int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
 
+/* No counterpart in the reference (a choice between two mappings of the same boundary kernel,
+   which give identical results).  kind 0: one thread per cell of the special list; kind 1: one warp
+   per cell, lane q doing direction q's reads; -1 (the default): kind 1 for lists of at most
+   LBFFS_SPECIAL_WARP_MAX cells, where one thread per cell leaves most SMs idle, else kind 0.
+   D3Q27 contexts always use kind 0. */
+#define LBFFS_SPECIAL_WARP_MAX 16384
+int lbffs_set_special_kernel(lbffs_ctx* ctx, int kind);
+
 /* setSolid + setNeiSolid (src/walls.hpp:159-216) on the device, bit for bit the reference's host
    result: solid[ic] = 1 for cells inside the closed surface (ray-crossing parity of isInner,
    walls.hpp:73-157, within the STL's bounding box, which the reference starts at the origin),

@@ -107,6 +107,7 @@ def load_library():
         "lbffs_cell_counts": ([vp, C.POINTER(C.c_longlong)], i),
         "lbffs_init_rest": ([vp], i),
         "lbffs_set_bulk_kernel": ([vp, i], i),
+        "lbffs_set_special_kernel": ([vp, i], i),
         "lbffs_voxelize": ([vp, C.POINTER(C.c_float), C.c_longlong, i], i),
         "lbffs_output": ([vp, C.POINTER(OutputParams), C.POINTER(OutputResult)], i),
         "lbffs_write_vtk": ([vp, C.c_char_p, i, C.POINTER(OutputParams)], i),
@@ -252,6 +253,11 @@ class Lattice:
     def set_bulk_kernel(self, kind):
         """D3Q19 bulk kernel variant: 0 per-thread loads, 1 row-staged bulk copies (same results)."""
         self._check(self.lib.lbffs_set_bulk_kernel(self.h, int(kind)))
+
+    def set_special_kernel(self, kind):
+        """Boundary kernel mapping: 0 one thread per listed cell, 1 one warp per cell, -1 by the list's
+        length (same results)."""
+        self._check(self.lib.lbffs_set_special_kernel(self.h, int(kind)))
 
     def init_rest(self):
         """Both population copies at rest (f_q = w_q) without a host upload."""

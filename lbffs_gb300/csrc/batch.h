@@ -14,7 +14,10 @@ struct BatchCase {
     long long nsteps;  // steps the case runs in total
     int slot;          // index of the case's step counter
     int seg_per_row;   // 32-cell x segments per row: ceil(nx / 32)
-    int tiles;         // bulk tiles of the case: ceil(seg_per_row * ny * nz / BATCH_SEG_PER_TILE)
+    int rowtile;       // 1: the case's bulk tiles are k_bulk's row tiles (bulk_block), 0: segments
+    int nxb;           // row tiles per row: ceil(nx / (BULK_BX * BULK_V))
+    int tiles;         // bulk tiles of the case: nxb * ny * nz row tiles, or
+                       // ceil(seg_per_row * ny * nz / BATCH_SEG_PER_TILE) segment tiles
     FastDiv dspr, dny;  // division by seg_per_row and by ny
 };
 
@@ -27,15 +30,22 @@ constexpr int BATCH_SEG_PER_TILE = (BULK_BX / 32) * BULK_V;
 #define LBFFS_BATCH_TILES 2
 #endif
 constexpr int BATCH_TILES_PER_CTA = LBFFS_BATCH_TILES;
+// cases whose rows fill at least 70 % of k_bulk's row tiles run in them (1), or every case in the
+// segment mapping (0); a build-time choice
+#ifndef LBFFS_BATCH_ROWTILE
+#define LBFFS_BATCH_ROWTILE 1
+#endif
 
-// Bulk step of every case in cases[0..ncases), in the segment mapping of bulk_segments (narrow
-// rows keep the lanes busy): CTA b runs run b - tile_start[c] of the case c
+// Bulk step of every case in cases[0..ncases), in k_bulk's row tiles (bulk_block) for wide rows and
+// in the segment mapping of bulk_segments (narrow rows keep the lanes busy) for the others: CTA b
+// runs run b - tile_start[c] of the case c
 // with tile_start[c] <= b < tile_start[c + 1] (prefix sums of runs of BATCH_TILES_PER_CTA tiles;
-// ntiles = tile_start[ncases] CTAs).
-cudaError_t batch_bulk(int storage, bool les, const BatchCase* cases, const int* tile_start, int ncases, int ntiles,
-                       const long long* done, cudaStream_t st);
-// Boundary step: thread t runs entry t - sp_start[c] of case c's special list.
-cudaError_t batch_special(int storage, const BatchCase* cases, const long long* sp_start, int ncases,
+// ntiles = tile_start[ncases] CTAs).  rows: the launch over the row-tile cases (the others count 0
+// tiles in its prefix sums), else over the segment cases.
+cudaError_t batch_bulk(int storage, bool les, bool rows, const BatchCase* cases, const int* tile_start, int ncases,
+                       int ntiles, const long long* done, cudaStream_t st);
+// Boundary step: thread (warp: warp) t runs entry t - sp_start[c] of case c's special list.
+cudaError_t batch_special(int storage, bool warp, const BatchCase* cases, const long long* sp_start, int ncases,
                           long long nspecial, const long long* done, cudaStream_t st);
 // Ghost layers: CTA b runs ghost-fill block b - h_start[c] of case c's source populations.
 cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nblocks,
@@ -44,14 +54,14 @@ cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_s
 cudaError_t batch_tick(const int* slots, const long long* nsteps, int n, long long* done, cudaStream_t st);
 
 // per storage format (batch_inst.cu compiled once per format)
-cudaError_t batch_bulk_s0(bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
-cudaError_t batch_bulk_s1(bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
-cudaError_t batch_bulk_s2(bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
-cudaError_t batch_special_s0(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s0(bool, bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s1(bool, bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s2(bool, bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
+cudaError_t batch_special_s0(bool, const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
 cudaError_t batch_halo_s0(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
 cudaError_t batch_halo_s1(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
 cudaError_t batch_halo_s2(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
-cudaError_t batch_special_s1(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
-cudaError_t batch_special_s2(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_special_s1(bool, const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_special_s2(bool, const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
 
 }  // namespace lbffs

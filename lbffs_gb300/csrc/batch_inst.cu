@@ -45,7 +45,9 @@ __device__ __forceinline__ int find_case(const T* __restrict__ start, int n, T k
 #define LBFFS_BATCH_ARGS_SMEM 0
 #endif
 
-template <bool LES>
+// ROWS: the cases in k_bulk's row tiles (BatchCase::rowtile), else those in the segment mapping; the
+// two mappings are separate kernels so that each keeps its own register allocation
+template <bool LES, bool ROWS>
 __global__ void LBFFS_BATCH_BOUNDS k_bulk_batch(const BatchCase* __restrict__ cases,
                                                         const int* __restrict__ tile_start, int ncases,
                                                         const long long* __restrict__ done)
@@ -77,12 +79,23 @@ __global__ void LBFFS_BATCH_BOUNDS k_bulk_batch(const BatchCase* __restrict__ ca
     const StepArgs& sa = d + 1 == cases[c].nsteps ? cases[c].last : cases[c].args[d & 1];
 #endif
     const int run = (int)blockIdx.x - tile_start[c];
-    const int spr = cases[c].seg_per_row, tiles = cases[c].tiles;
-    const int nseg = spr * sa.ny * sa.nz;
+    const int tiles = cases[c].tiles;
     const int t1 = min(tiles, (run + 1) * BATCH_TILES_PER_CTA);
-    for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++)
-        bulk_segments<19, S, COLL_RR, SGS_SMAG, LES>(sa, tile * BATCH_SEG_PER_TILE, spr, nseg, cases[c].dspr,
-                                                     cases[c].dny);
+    if constexpr (ROWS) {
+        // wide rows: k_bulk's own row tiles (the same pair paths, without its launch-order prefetch)
+        const int nxb = cases[c].nxb;
+        for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++) {
+            const int r = tile / nxb;
+            const int k = (int)fdiv(r, cases[c].dny);
+            bulk_block<19, S, COLL_RR, SGS_SMAG, LES, false>(sa, tile - r * nxb, r - k * sa.ny, k);
+        }
+    } else {
+        const int spr = cases[c].seg_per_row;
+        const int nseg = spr * sa.ny * sa.nz;
+        for (int tile = run * BATCH_TILES_PER_CTA; tile < t1; tile++)
+            bulk_segments<19, S, COLL_RR, SGS_SMAG, LES>(sa, tile * BATCH_SEG_PER_TILE, spr, nseg, cases[c].dspr,
+                                                         cases[c].dny);
+    }
 }
 
 __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* __restrict__ cases,
@@ -95,6 +108,19 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* _
     const long long d = done[cases[c].slot];
     if (d >= cases[c].nsteps) return;
     special_cell<19, S, COLL_RR>(cases[c].args[d & 1], t - sp_start[c]);
+}
+
+// one warp per listed cell (special_cell with WARP), for short lists
+__global__ void __launch_bounds__(SPECIAL_BS) k_special_batch_warp(const BatchCase* __restrict__ cases,
+                                                                   const long long* __restrict__ sp_start,
+                                                                   int ncases, const long long* __restrict__ done)
+{
+    const long long t = (long long)blockIdx.x * (SPECIAL_BS / 32) + (threadIdx.x >> 5);
+    if (t >= sp_start[ncases]) return;
+    const int c = find_case<long long>(sp_start, ncases, t);
+    const long long d = done[cases[c].slot];
+    if (d >= cases[c].nsteps) return;
+    special_cell<19, S, COLL_RR, true>(cases[c].args[d & 1], t - sp_start[c]);
 }
 
 using W = typename std::conditional<S == ST_FP32, uint32_t, uint16_t>::type;
@@ -119,19 +145,31 @@ __global__ void __launch_bounds__(HALO_BS) k_halo_batch(const BatchCase* __restr
 #define LBFFS_CAT2(a, b) a##b
 #define LBFFS_CAT(a, b) LBFFS_CAT2(a, b)
 
-cudaError_t LBFFS_CAT(batch_bulk_s, LBFFS_S)(bool les, const BatchCase* cases, const int* tile_start, int ncases,
-                                             int ntiles, const long long* done, cudaStream_t st)
+cudaError_t LBFFS_CAT(batch_bulk_s, LBFFS_S)(bool les, bool rows, const BatchCase* cases, const int* tile_start,
+                                             int ncases, int ntiles, const long long* done, cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    if (les) k_bulk_batch<true><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
-    else k_bulk_batch<false><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+    if (rows) {
+        if (les) k_bulk_batch<true, true><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+        else k_bulk_batch<false, true><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+    } else {
+        if (les) k_bulk_batch<true, false><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+        else k_bulk_batch<false, false><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t LBFFS_CAT(batch_special_s, LBFFS_S)(const BatchCase* cases, const long long* sp_start, int ncases,
-                                                long long nspecial, const long long* done, cudaStream_t st)
+cudaError_t LBFFS_CAT(batch_special_s, LBFFS_S)(bool warp, const BatchCase* cases, const long long* sp_start,
+                                                int ncases, long long nspecial, const long long* done,
+                                                cudaStream_t st)
 {
     if (nspecial <= 0) return cudaSuccess;
+    if (warp) {
+        constexpr int per = SPECIAL_BS / 32;
+        k_special_batch_warp<<<(unsigned)((nspecial + per - 1) / per), SPECIAL_BS, 0, st>>>(cases, sp_start, ncases,
+                                                                                            done);
+        return cudaGetLastError();
+    }
     const unsigned nb = (unsigned)((nspecial + SPECIAL_BS - 1) / SPECIAL_BS);
     k_special_batch<<<nb, SPECIAL_BS, 0, st>>>(cases, sp_start, ncases, done);
     return cudaGetLastError();

@@ -80,6 +80,7 @@ struct lbffs_ctx {
     // timing
     bool timing = false;
     int bulk_kind = 0;  // D3Q19 bulk kernel variant (lbffs_set_bulk_kernel)
+    int special_kind = -1;  // boundary kernel mapping (lbffs_set_special_kernel): -1 by list length
     struct Ev {
         cudaEvent_t a, b;
         int kind;

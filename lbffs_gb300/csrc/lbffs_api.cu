@@ -639,6 +639,11 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
     a.tau_n = mn[4];
     a.store_all = p->store_fields == 2;
     a.bulk_kind = c->Q == 19 ? c->bulk_kind : 0;
+    // the warp mapping is built for D3Q19
+    a.special_kind = c->Q != 19                ? 0
+                     : c->special_kind >= 0    ? c->special_kind
+                     : c->n_special <= LBFFS_SPECIAL_WARP_MAX ? 1
+                                                              : 0;
     a.l2_policy = 2LL * c->Q * c->pg.pE * c->tsize <= c->l2_bytes ? 1 : 0;
 }
 
@@ -998,5 +1003,13 @@ extern "C" int lbffs_set_bulk_kernel(lbffs_ctx* c, int kind)
 {
     if (!c || kind < 0 || kind > 1) return fail(c, LBFFS_E_ARG, "lbffs_set_bulk_kernel: kind must be 0 or 1");
     c->bulk_kind = kind;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_set_special_kernel(lbffs_ctx* c, int kind)
+{
+    if (!c || kind < -1 || kind > 1)
+        return fail(c, LBFFS_E_ARG, "lbffs_set_special_kernel: kind must be -1, 0 or 1");
+    c->special_kind = kind;
     return LBFFS_OK;
 }

@@ -64,11 +64,11 @@ struct Group {
     bool les = false;
     std::vector<Request*> members;
     BatchCase* d_cases = nullptr;
-    int* d_tiles = nullptr;
+    int* d_tiles = nullptr;  // prefix sums of bulk CTAs: segment cases [0, n], then row-tile cases
     long long* d_sp = nullptr;
     long long* d_halo = nullptr;
     size_t cap = 0;
-    int ntiles = 0;
+    int ntiles = 0, ntiles_rows = 0;
     long long nspecial = 0, nhalo = 0;
 };
 
@@ -270,12 +270,13 @@ cudaError_t build_batch(lbffs_server* s)
         const int n = (int)g.members.size();
         if (n == 0) {
             g.ntiles = 0;
+            g.ntiles_rows = 0;
             g.nspecial = 0;
             g.nhalo = 0;
             continue;
         }
         std::vector<BatchCase> hc(n);
-        std::vector<int> tiles(n + 1, 0);
+        std::vector<int> tiles(2 * (n + 1), 0);  // segment cases, then row-tile cases
         std::vector<long long> sp(n + 1, 0), hl(n + 1, 0);
         for (int i = 0; i < n; i++) {
             Request* r = g.members[i];
@@ -294,9 +295,16 @@ cudaError_t build_batch(lbffs_server* s)
             hc[i].seg_per_row = (c->d.nx + 31) / 32;
             hc[i].dspr = fast_div((uint32_t)hc[i].seg_per_row);
             hc[i].dny = fast_div((uint32_t)c->d.ny);
-            hc[i].tiles = (int)(((long long)hc[i].seg_per_row * c->d.ny * c->d.nz + BATCH_SEG_PER_TILE - 1) /
-                                BATCH_SEG_PER_TILE);
-            tiles[i + 1] = tiles[i] + (hc[i].tiles + BATCH_TILES_PER_CTA - 1) / BATCH_TILES_PER_CTA;
+            // rows that fill most of k_bulk's row tiles run in them (the paths lbffs_step runs);
+            // narrow rows in 32-cell segments packed across rows
+            hc[i].nxb = (c->d.nx + BULK_BX * BULK_V - 1) / (BULK_BX * BULK_V);
+            hc[i].rowtile = LBFFS_BATCH_ROWTILE && 10 * c->d.nx >= 7 * BULK_BX * BULK_V * hc[i].nxb;
+            hc[i].tiles = hc[i].rowtile ? hc[i].nxb * c->d.ny * c->d.nz
+                                        : (int)(((long long)hc[i].seg_per_row * c->d.ny * c->d.nz +
+                                                 BATCH_SEG_PER_TILE - 1) / BATCH_SEG_PER_TILE);
+            const int ctas = (hc[i].tiles + BATCH_TILES_PER_CTA - 1) / BATCH_TILES_PER_CTA;
+            tiles[i + 1] = tiles[i] + (hc[i].rowtile ? 0 : ctas);
+            tiles[n + 2 + i] = tiles[n + 1 + i] + (hc[i].rowtile ? ctas : 0);
             sp[i + 1] = sp[i] + c->n_special;
             hl[i + 1] = hl[i] + halo_blocks(c->pg, 19, 0) + halo_blocks(c->pg, 19, 1) + halo_blocks(c->pg, 19, 2);
         }
@@ -308,20 +316,22 @@ cudaError_t build_batch(lbffs_server* s)
             if (g.d_halo) cudaFree(g.d_halo);
             cap = (size_t)(n + 1) * 2;
             if ((e = cudaMalloc(&g.d_cases, sizeof(BatchCase) * cap)) != cudaSuccess) return e;
-            if ((e = cudaMalloc(&g.d_tiles, sizeof(int) * cap)) != cudaSuccess) return e;
+            if ((e = cudaMalloc(&g.d_tiles, sizeof(int) * 2 * cap)) != cudaSuccess) return e;
             if ((e = cudaMalloc(&g.d_sp, sizeof(long long) * cap)) != cudaSuccess) return e;
             if ((e = cudaMalloc(&g.d_halo, sizeof(long long) * cap)) != cudaSuccess) return e;
             g.cap = cap;
         }
         if ((e = cudaMemcpyAsync(g.d_cases, hc.data(), sizeof(BatchCase) * n, cudaMemcpyHostToDevice, s->stream)))
             return e;
-        if ((e = cudaMemcpyAsync(g.d_tiles, tiles.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s->stream)))
+        if ((e = cudaMemcpyAsync(g.d_tiles, tiles.data(), sizeof(int) * 2 * (n + 1), cudaMemcpyHostToDevice,
+                                 s->stream)))
             return e;
         if ((e = cudaMemcpyAsync(g.d_sp, sp.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, s->stream)))
             return e;
         if ((e = cudaMemcpyAsync(g.d_halo, hl.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, s->stream)))
             return e;
         g.ntiles = tiles[n];
+        g.ntiles_rows = tiles[2 * n + 1];
         g.nspecial = sp[n];
         g.nhalo = hl[n];
     }
@@ -359,14 +369,18 @@ cudaError_t build_batch(lbffs_server* s)
             if (le == cudaSuccess) le = cudaStreamWaitEvent(s->branch, s->fork_ev, 0);
             for (Group& g : s->groups)
                 if (le == cudaSuccess && g.nspecial > 0)
-                    le = batch_special(g.storage, g.d_cases, g.d_sp, (int)g.members.size(), g.nspecial, s->d_done,
-                                       s->branch);
+                    le = batch_special(g.storage, g.nspecial <= LBFFS_SPECIAL_WARP_MAX, g.d_cases, g.d_sp,
+                                       (int)g.members.size(), g.nspecial, s->d_done, s->branch);
             if (le == cudaSuccess) le = cudaEventRecord(s->join_ev, s->branch);
         }
-        for (Group& g : s->groups)
-            if (le == cudaSuccess && g.ntiles > 0)
-                le = batch_bulk(g.storage, g.les, g.d_cases, g.d_tiles, (int)g.members.size(), g.ntiles, s->d_done,
+        for (Group& g : s->groups) {
+            const int n = (int)g.members.size();
+            if (le == cudaSuccess && g.ntiles_rows > 0)
+                le = batch_bulk(g.storage, g.les, true, g.d_cases, g.d_tiles + n + 1, n, g.ntiles_rows, s->d_done,
                                 s->stream);
+            if (le == cudaSuccess && g.ntiles > 0)
+                le = batch_bulk(g.storage, g.les, false, g.d_cases, g.d_tiles, n, g.ntiles, s->d_done, s->stream);
+        }
         if (le == cudaSuccess && any_special) le = cudaStreamWaitEvent(s->stream, s->join_ev, 0);
         if (le == cudaSuccess) le = batch_tick(s->d_tick_slots, s->d_tick_nsteps, s->ntick, s->d_done, s->stream);
     }
@@ -555,13 +569,13 @@ cudaError_t batch_tick(const int* slots, const long long* nsteps, int n, long lo
     return cudaGetLastError();
 }
 
-cudaError_t batch_bulk(int storage, bool les, const BatchCase* cases, const int* tile_start, int ncases, int ntiles,
-                       const long long* done, cudaStream_t st)
+cudaError_t batch_bulk(int storage, bool les, bool rows, const BatchCase* cases, const int* tile_start, int ncases,
+                       int ntiles, const long long* done, cudaStream_t st)
 {
     switch (storage) {
-        case ST_FP32: return batch_bulk_s0(les, cases, tile_start, ncases, ntiles, done, st);
-        case ST_FP16S: return batch_bulk_s1(les, cases, tile_start, ncases, ntiles, done, st);
-        case ST_BF16S: return batch_bulk_s2(les, cases, tile_start, ncases, ntiles, done, st);
+        case ST_FP32: return batch_bulk_s0(les, rows, cases, tile_start, ncases, ntiles, done, st);
+        case ST_FP16S: return batch_bulk_s1(les, rows, cases, tile_start, ncases, ntiles, done, st);
+        case ST_BF16S: return batch_bulk_s2(les, rows, cases, tile_start, ncases, ntiles, done, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -577,13 +591,13 @@ cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_s
     return cudaErrorInvalidValue;
 }
 
-cudaError_t batch_special(int storage, const BatchCase* cases, const long long* sp_start, int ncases,
+cudaError_t batch_special(int storage, bool warp, const BatchCase* cases, const long long* sp_start, int ncases,
                           long long nspecial, const long long* done, cudaStream_t st)
 {
     switch (storage) {
-        case ST_FP32: return batch_special_s0(cases, sp_start, ncases, nspecial, done, st);
-        case ST_FP16S: return batch_special_s1(cases, sp_start, ncases, nspecial, done, st);
-        case ST_BF16S: return batch_special_s2(cases, sp_start, ncases, nspecial, done, st);
+        case ST_FP32: return batch_special_s0(warp, cases, sp_start, ncases, nspecial, done, st);
+        case ST_FP16S: return batch_special_s1(warp, cases, sp_start, ncases, nspecial, done, st);
+        case ST_BF16S: return batch_special_s2(warp, cases, sp_start, ncases, nspecial, done, st);
     }
     return cudaErrorInvalidValue;
 }

@@ -19,6 +19,14 @@ cudaError_t LBFFS_NAME(LBFFS_Q, LBFFS_S, LBFFS_C, LBFFS_PART)(const StepArgs& a,
 {
 #if LBFFS_PART == 3
     if (a.n_special <= 0) return cudaSuccess;
+#if LBFFS_Q == 19
+    if (a.special_kind == 1) {
+        constexpr int per = SPECIAL_BS / 32;
+        const dim3 grid((unsigned)((a.n_special + per - 1) / per));
+        k_special_warp<LBFFS_Q, LBFFS_S, LBFFS_C><<<grid, SPECIAL_BS, 0, st>>>(a);
+        return cudaGetLastError();
+    }
+#endif
     const dim3 grid((unsigned)((a.n_special + SPECIAL_BS - 1) / SPECIAL_BS));
     k_special<LBFFS_Q, LBFFS_S, LBFFS_C><<<grid, SPECIAL_BS, 0, st>>>(a);
 #else

@@ -863,8 +863,9 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
 // instruction of a warp covers 32 consecutive cells.  Every population is pulled from the same
 // offset for every cell: cells on the domain border read the ghost layer, which k_halo filled
 // with the reference's face streaming at the start of the step.
-// One CTA tile: BULK_BX * bulk_v<Q>() cells of row (j, k) starting at x-block xb.
-template <int Q, int S, int COLL, int SGS, bool LES>
+// One CTA tile: BULK_BX * bulk_v<Q>() cells of row (j, k) starting at x-block xb.  PF: the tile is
+// CTA (xb, j, k) of a k_bulk grid, so the L2 prefetch of the tiles launched later may run.
+template <int Q, int S, int COLL, int SGS, bool LES, bool PF = true>
 __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int k)
 {
     using T = typename Codec<S>::T;
@@ -882,7 +883,7 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     constexpr int DV = ADJ ? 1 : 32;  // x distance of a lane's consecutive cells
     const int row = (k * a.ny + j) * a.nx;
     const int prow = pidx(a, 0, j, k);
-    bulk_prefetch<Q, S, V>(a);
+    if constexpr (PF) bulk_prefetch<Q, S, V>(a);
     if constexpr (PAIR27) {
         if constexpr (S != ST_FP32) bulk_pair_adj_eager<S, LES, 27>(a, base + 2 * lane, j, k, row, prow);
         else bulk_pair_eager<S, LES, 27>(a, base + lane, j, k, row, prow);
@@ -969,6 +970,54 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
         const int k = fdiv(row, dny), j = row - k * a.ny;
         bulk_pair_adj_eager<S, LES>(a, inrange ? i0 : a.nx, j, k, row * a.nx, pidx(a, 0, j, k), inrange);
         return;
+    } else if constexpr (Q == 19 && SGS != SGS_WALE && BULK_V == 2 && LBFFS_BULK_EAGER32) {
+        // FP32: lane l takes cell l of both segments, its pulls issued together with the flag loads
+        // (as bulk_pair_eager does for a row tile)
+        int ci[2], cj[2], ck[2], ic[2], ip[2];
+        bool valid[2];
+        uint8_t fl[2];
+#pragma unroll
+        for (int v = 0; v < 2; v++) {
+            const int g = g0 + warp * 2 + v;
+            const int row = g < nseg ? fdiv(g, dspr) : 0;
+            ci[v] = (g - row * spr) * 32 + lane;
+            valid[v] = g < nseg && ci[v] < a.nx;
+            ck[v] = fdiv(row, dny);
+            cj[v] = row - ck[v] * a.ny;
+            ic[v] = row * a.nx + ci[v];
+            ip[v] = pidx(a, ci[v], cj[v], ck[v]);
+            fl[v] = valid[v] ? __ldg(a.flags + ic[v]) : FL_SOLID;
+        }
+        F2 ft[19];
+        if (row_crosses(a, cj[0], ck[0]) || row_crosses(a, cj[1], ck[1])) {
+            const BorderCell rb[2] = {row_border(a, cj[0], ck[0]), row_border(a, cj[1], ck[1])};
+            const T* f = static_cast<const T*>(a.f_in);
+#pragma unroll
+            for (int q = 0; q < 19; q++) {
+                const float x0 = valid[0] ? Codec<S>::load_held(f + border_pull<19>(a, rb[0], q, ip[0])) : 0.f;
+                const float x1 = valid[1] ? Codec<S>::load_held(f + border_pull<19>(a, rb[1], q, ip[1])) : 0.f;
+                ft[q] = pk(x0, x1);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 19; q++) {
+                const T* p = static_cast<const T*>(a.fin_s[q]);
+                const float x0 = valid[0] ? Codec<S>::load_held(p + ip[0]) : 0.f;
+                const float x1 = valid[1] ? Codec<S>::load_held(p + ip[1]) : 0.f;
+                ft[q] = pk(x0, x1);
+            }
+        }
+        const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
+        const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act));
+        if (!(act[0] || act[1])) return;
+        bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+#pragma unroll
+        for (int q = 0; q < 19; q++) {
+            T* p = static_cast<T*>(a.fout_q[q]);
+            if (act[0]) Codec<S>::store_held(p + ip[0], lane0(ft[q]));
+            if (act[1]) Codec<S>::store_held(p + ip[1], lane1(ft[q]));
+        }
+        return;
     }
     int ci[BULK_V], cj[BULK_V], ck[BULK_V];
     uint8_t fl[BULK_V];
@@ -1041,8 +1090,81 @@ __global__ void LBFFS_BULK_BOUNDS(Q) k_bulk(const StepArgs a)
     bulk_block<Q, S, COLL, SGS, LES>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
-// The general boundary path of entry t of the special list.
-template <int Q, int S, int COLL>
+// ---- one warp per boundary cell (special_cell with WARP) ----
+// Lane q < Q of the warp does the per-direction memory work of direction q: its pull, its own
+// previous value, the outlet's inner value and the STL link's reads, all issued in one round trip
+// after the cell index; the values are exchanged by shuffles and the operators run on the full
+// population set in every lane, so the cell's arithmetic is the thread version's.
+
+// velocity, opposite direction and weight of direction q (q at run time)
+template <int Q>
+struct LaneDir {
+    int c[3];
+    int opp;
+    float w;
+};
+template <int Q>
+__device__ __forceinline__ LaneDir<Q> lane_dir(int q)
+{
+    LaneDir<Q> r{{0, 0, 0}, 0, 0.f};
+#pragma unroll
+    for (int p = 0; p < Q; p++)
+        if (q == p) {
+            r.c[0] = lat_c(Q, p, 0);
+            r.c[1] = lat_c(Q, p, 1);
+            r.c[2] = lat_c(Q, p, 2);
+            r.opp = lat_opp(Q, p);
+            r.w = lat_w(Q, p);
+        }
+    return r;
+}
+
+// upwind<Q> for a direction given by its velocity c (run time)
+__device__ __forceinline__ long long upwind_c(const int (&c)[3], const int (&x)[3], const int (&N)[3], const int (&b)[3],
+                                              bool face)
+{
+    int n[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        n[d] = x[d] - c[d];
+        if (n[d] < 0) {
+            if (face && is_wall_code(b[d])) return -1;
+            n[d] += N[d];
+        } else if (n[d] >= N[d]) {
+            if (face && is_wall_code(b[d])) return -1;
+            n[d] -= N[d];
+        }
+    }
+    return ((long long)n[2] * N[1] + n[1]) * N[0] + n[0];
+}
+
+// border_pull<Q> for direction q with velocity c and missing direction m given at run time
+__device__ __forceinline__ long long border_pull_c(const StepArgs& a, const BorderCell& g, const int (&c)[3], int q,
+                                                   int m, int ip)
+{
+    int shift = 0;
+    bool out = false, wall = false;
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        if (c[e] > 0 && g.lo[e]) {
+            out = true;
+            shift += g.wrap[e];
+            wall |= is_wall_code(g.b[e]);
+        } else if (c[e] < 0 && g.hi[e]) {
+            out = true;
+            shift -= g.wrap[e];
+            wall |= is_wall_code(g.b[e]);
+        }
+    }
+    const long long pull = (long long)q * a.pE + (ip - (c[0] + c[1] * a.px + c[2] * a.pxy));
+    if (!out) return pull;
+    if (!(g.face && wall)) return pull + shift;
+    return (long long)m * a.pE + ip;
+}
+
+// The general boundary path of entry t of the special list: one thread per cell, or (WARP) one
+// warp per cell, every lane calling with the same t.
+template <int Q, int S, int COLL, bool WARP = false>
 __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
 {
     using T = typename Codec<S>::T;
@@ -1074,8 +1196,98 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     // streaming: upwind value, or the face rule's value (upwindID_B + reflectOrMirrorQ): from the
     // ghost that holds it (filled by k_halo), or, with border pulls, read where the rule takes it
     float ft[Q];
-    if (a.border_pulls && (x[0] == 0 || x[0] == N[0] - 1 || x[1] == 0 || x[1] == N[1] - 1 || x[2] == 0 ||
-                           x[2] == N[2] - 1)) {
+    [[maybe_unused]] const int lane = threadIdx.x & 31;
+    [[maybe_unused]] const int lq = lane < Q ? lane : 0;  // lanes >= Q stand in for direction 0
+    [[maybe_unused]] LaneDir<Q> ld;
+    // WARP: this lane's outlet value and STL-link result with its momentum-exchange sum fb + f_q
+    // (lanes 1..Q-1)
+    [[maybe_unused]] float v_out = 0.f, v_link = 0.f, v_fw = 0.f;
+    [[maybe_unused]] bool has_out = false, link = false;
+    if constexpr (WARP) {
+        ld = lane_dir<Q>(lq);
+        const T* fin = static_cast<const T*>(a.f_in);
+        long long el;
+        if (a.border_pulls && (x[0] == 0 || x[0] == N[0] - 1 || x[1] == 0 || x[1] == N[1] - 1 || x[2] == 0 ||
+                               x[2] == N[2] - 1)) {
+            const BorderCell g = border_cell(a, x[0], x[1], x[2]);
+            int m = 0;
+#pragma unroll
+            for (int p = 0; p < Q; p++)
+                if (lq == p) m = missing_dir<Q>(p, g.b);
+            el = border_pull_c(a, g, ld.c, lq, m, ip);
+        } else {
+            el = (long long)lq * a.pE + (ip - (ld.c[0] + ld.c[1] * a.px + ld.c[2] * a.pxy));
+        }
+        const float fs = Codec<S>::load(fin + el, ld.w);
+        const float fo = Codec<S>::load(fin + (long long)lq * a.pE + ip, ld.w);  // the cell's own previous f_q
+        // outflowBC's inner value (the last outlet face of the cell whose inward direction q is)
+        float f_in_cell = 0.f;
+        int out_axis = 0;
+        if (face && (b[0] == BC_OUTLET || b[1] == BC_OUTLET || b[2] == BC_OUTLET)) {
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                if (b[d] != BC_OUTLET) continue;
+#pragma unroll
+                for (int side = -1; side <= 1; side += 2) {
+                    if (!((side < 0 && x[d] == 0) || (side > 0 && x[d] == N[d] - 1))) continue;
+                    if (lane >= 1 && lane < Q && ld.c[d] == -side) {
+                        f_in_cell = Codec<S>::load(fin + (long long)lq * a.pE + inner_p(d, side), ld.w);
+                        has_out = true;
+                        out_axis = d;
+                    }
+                }
+            }
+        }
+        // STL link of direction q (internalWallBC): its reads, before the link test resolves
+        const bool nei = a.nei_solid[ic] == 1;
+        float fb = 0.f, sdf1 = 0.f, ufc[3] = {0.f, 0.f, 0.f};
+        if (nei && lane >= 1 && lane < Q) {
+            const long long up = upwind_c(ld.c, x, N, b, face);
+            link = up >= 0 && a.solid[up] == 1;
+            // F(opposite of q, ip); opposite directions have equal weights
+            fb = Codec<S>::load(fin + (long long)ld.opp * a.pE + ip, ld.w);
+            if (a.wall != WALL_BB) {
+                sdf1 = up >= 0 ? a.sdf[up] : 0.f;
+                const int cb[3] = {-ld.c[0], -ld.c[1], -ld.c[2]};
+                const long long fl = upwind_c(cb, x, N, b, face);
+                const long long fc = fl < 0 ? ic : fl;
+                ufc[0] = a.u_p[fc];
+                ufc[1] = a.v_p[fc];
+                ufc[2] = a.w_p[fc];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < Q; q++) ft[q] = __shfl_sync(0xffffffffu, fs, q);
+        const float uo_[3] = {a.u_p[ic], a.v_p[ic], a.w_p[ic]};
+        if (has_out) {
+            const float g = 0.57735026919f - (out_axis == 0 ? uo_[0] : out_axis == 1 ? uo_[1] : uo_[2]);
+            v_out = g * f_in_cell + (1.f - g) * fo;
+        }
+        if (link) {
+            if (a.wall == WALL_BB) {
+                v_link = fb;
+            } else {
+                const float omega_l = a.omega[ic], rho_o = a.rho_p[ic], tau_o = a.tau_p[ic];
+                const float usq = uo_[0] * uo_[0] + uo_[1] * uo_[1] + uo_[2] * uo_[2];
+                const float sdf0 = a.sdf[ic];
+                const float qf = fabsf(sdf0) / (fabsf(sdf0) + fabsf(sdf1));
+                const float we = 1.f / (1.f / omega_l + tau_o);
+                const float uc = -uo_[0] * (float)ld.c[0] - uo_[1] * (float)ld.c[1] - uo_[2] * (float)ld.c[2];
+                float feq, chi;
+                if (qf <= 0.5f) {
+                    const float uf = -ufc[0] * (float)ld.c[0] - ufc[1] * (float)ld.c[1] - ufc[2] * (float)ld.c[2];
+                    feq = (rho_o + 3.f * uf + 4.5f * uc * uc - 1.5f * usq) * ld.w;
+                    chi = we * (2.f * qf - 1.f) / (1.f - 2.f * we);
+                } else {
+                    feq = (rho_o + 3.f * (1.f - 1.f / qf) * uc + 4.5f * uc * uc - 1.5f * usq) * ld.w;
+                    chi = we * (2.f * qf - 1.f);
+                }
+                v_link = (1.f - chi) * fb + chi * feq;
+            }
+            v_fw = fb + v_link;
+        }
+    } else if (a.border_pulls && (x[0] == 0 || x[0] == N[0] - 1 || x[1] == 0 || x[1] == N[1] - 1 || x[2] == 0 ||
+                                  x[2] == N[2] - 1)) {
         const BorderCell g = border_cell(a, x[0], x[1], x[2]);
 #pragma unroll
         for (int q = 0; q < Q; q++)
@@ -1205,7 +1417,14 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
             }
         }
         // outflowBC (Geier et al. 2015 App. F; kernel.cl:2005-2097)
-        if (b[0] == BC_OUTLET || b[1] == BC_OUTLET || b[2] == BC_OUTLET) {
+        if constexpr (WARP) {
+            // the lanes' outlet values (computed from the same reads as below)
+#pragma unroll
+            for (int q = 1; q < Q; q++) {
+                const float vq = __shfl_sync(0xffffffffu, v_out, q);
+                if (__shfl_sync(0xffffffffu, (int)has_out, q)) ft[q] = vq;
+            }
+        } else if (b[0] == BC_OUTLET || b[1] == BC_OUTLET || b[2] == BC_OUTLET) {
             const float cs = 0.57735026919f;
 #pragma unroll
             for (int d = 0; d < 3; d++) {
@@ -1228,7 +1447,22 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     // internalWallBC: STL links (kernel.cl:1926-2003 / D3Q27 1823-1897)
     float fw[3] = {0.f, 0.f, 0.f};
     const float omega = a.omega[ic];
-    if (a.nei_solid[ic] == 1) {
+    if constexpr (WARP) {
+        // the lanes' link results, and the momentum exchange summed in direction order
+        if (__any_sync(0xffffffffu, link)) {
+#pragma unroll
+            for (int q = 1; q < Q; q++) {
+                const float vq = __shfl_sync(0xffffffffu, v_link, q);
+                const float sq = __shfl_sync(0xffffffffu, v_fw, q);
+                if (__shfl_sync(0xffffffffu, (int)link, q)) {
+                    ft[q] = vq;
+#pragma unroll
+                    for (int d = 0; d < 3; d++)
+                        if (lat_c(Q, q, d)) fw[d] += -sq * (float)lat_c(Q, q, d);
+                }
+            }
+        }
+    } else if (a.nei_solid[ic] == 1) {
         const float rho_o = a.rho_p[ic], tau_o = a.tau_p[ic];
         const float usq = uo[0] * uo[0] + uo[1] * uo[1] + uo[2] * uo[2];
 #pragma unroll
@@ -1263,9 +1497,11 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
                 if (lat_c(Q, q, d)) fw[d] += -(fb + ft[q]) * (float)lat_c(Q, q, d);
         }
     }
-    a.fwx[ic] = fw[0];
-    a.fwy[ic] = fw[1];
-    a.fwz[ic] = fw[2];
+    if (!WARP || lane == 0) {
+        a.fwx[ic] = fw[0];
+        a.fwy[ic] = fw[1];
+        a.fwz[ic] = fw[2];
+    }
 
     float rho, u, v, w, tsgs = 0.f;
     Mom19 m19;
@@ -1287,12 +1523,14 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
         else tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
         tsgs = damping(a, tsgs, a.sdf[ic], u, v, w, omega);
     }
-    a.rho_n[ic] = rho;
-    a.u_n[ic] = u;
-    a.v_n[ic] = v;
-    a.w_n[ic] = w;
-    a.tau_n[ic] = tsgs;
-    if (a.err && !(rho == rho)) atomicOr(a.err, 1);
+    if (!WARP || lane == 0) {
+        a.rho_n[ic] = rho;
+        a.u_n[ic] = u;
+        a.v_n[ic] = v;
+        a.w_n[ic] = w;
+        a.tau_n[ic] = tsgs;
+        if (a.err && !(rho == rho)) atomicOr(a.err, 1);
+    }
     const float tau = sponge_tau(a, 1.f / omega, tsgs, x[0], x[1], x[2]);
     if constexpr (Q == 19) {
         const float U[3] = {u - 0.5f * a.dpdx / rho, v, w};
@@ -1300,8 +1538,16 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     } else {
         collide<Q, COLL>(ft, rho, u, v, w, 1.f / (tau + tsgs), a);
     }
+    if constexpr (WARP) {
+        float mine = ft[0];
 #pragma unroll
-    for (int q = 0; q < Q; q++) Codec<S>::store(static_cast<T*>(a.fout_q[q]) + ip, ft[q], lat_w(Q, q));
+        for (int q = 1; q < Q; q++)
+            if (lane == q) mine = ft[q];
+        if (lane < Q) Codec<S>::store(static_cast<T*>(a.f_out) + (long long)lane * a.pE + ip, mine, ld.w);
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) Codec<S>::store(static_cast<T*>(a.fout_q[q]) + ip, ft[q], lat_w(Q, q));
+    }
 }
 
 template <int Q, int S, int COLL>
@@ -1309,6 +1555,15 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
 {
     const long long t = (long long)blockIdx.x * SPECIAL_BS + threadIdx.x;
     if (t < a.n_special) special_cell<Q, S, COLL>(a, t);
+}
+
+// one warp per listed cell (special_cell with WARP): for short lists, where one thread per cell
+// leaves most SMs idle and each thread's chain of dependent reads sets the kernel's time
+template <int Q, int S, int COLL>
+__global__ void __launch_bounds__(SPECIAL_BS) k_special_warp(const StepArgs a)
+{
+    const long long t = (long long)blockIdx.x * (SPECIAL_BS / 32) + (threadIdx.x >> 5);
+    if (t < a.n_special) special_cell<Q, S, COLL, true>(a, t);
 }
 
 // ---- ghost layer: the reference's face streaming for populations that cross the grid edge ----

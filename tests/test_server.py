@@ -147,6 +147,25 @@ def test_serving_workload_sample_matches_plain_lattices(cuda_lib):
     assert not bad, bad
 
 
+def test_wide_rows_run_in_row_tiles_and_equal_lattice(cuda_lib):
+    """Cases whose rows fill most of a 256-cell row tile (nx >= 180) run in the single-lattice kernel's
+    row tiles inside the batch, next to narrow cases in the segment mapping: every served field
+    equals the plain Lattice run."""
+    from lbffs_gb300.serve import Server
+    wide_ch = _channel(192, 24, 6)
+    wide_cav = K.make_case(200, 12, 10, 19, K.cavity_faces(0.05), nu=0.03)
+    two_tiles = _channel(300, 16, 4)
+    runs = [(wide_ch, 30, "fp32", "ibb"), (wide_ch, 23, "fp16s", "ibb"), (wide_cav, 27, "fp32", "bb"),
+            (wide_cav, 31, "fp16s", "bb"), (two_tiles, 19, "fp16s", "ibb"), (_cavity(20, 0.05, 0.02), 25, "fp32", "bb")]
+    with Server(hbm_budget=1 << 30, max_cases=8, steps_per_round=8) as srv:
+        ids = [srv.submit(c, n, st, wall=w) for c, n, st, w in runs]
+        for cid in ids:
+            srv.wait(cid)
+        served = [_served_fields(srv, cid) for cid in ids]
+    for k, (c, n, st, w) in enumerate(runs):
+        assert _same(served[k], _lattice_fields(c, n, st, w)), (k, c.nx, st)
+
+
 def test_slot_reuse_under_continuous_admission(cuda_lib):
     """Two slots and one step per round, so every round retires a case and admits the next into
     the slot just freed while the batch of the other slot runs: each served result equals the
