@@ -236,16 +236,20 @@ def _serial(reqs, cases, device, per_step_sync):
     return time.perf_counter() - t0, lat_ms, keep
 
 
-def run_serving(n_req, step_scale, device, budget_gb=150.0):
-    """Served (continuous batching) vs serial plain launches of the same requests and arrivals."""
+def run_serving(n_req, step_scale, device, budget_gb=150.0, serial=True):
+    """Served (continuous batching) vs serial plain launches of the same requests and arrivals
+    (serial=False: the served run alone)."""
     from lbffs_gb300.serve import Server
     reqs = serving_requests(n_req, step_scale)
     cases = [serving_case(r) for r in reqs]
     cells = [c.nx * c.ny * c.nz * r["steps"] for r, (c, _) in zip(reqs, cases)]
     bpc = [BYTES_PER_CELL[(19, r["storage"])] for r in reqs]
 
-    t_plain, lat_plain, keep = _serial(reqs, cases, device, True)
-    t_async, lat_async, _ = _serial(reqs, cases, device, False)
+    if serial:
+        t_plain, lat_plain, keep = _serial(reqs, cases, device, True)
+        t_async, lat_async, _ = _serial(reqs, cases, device, False)
+    else:
+        t_plain, lat_plain, keep, t_async = float("nan"), [float("nan")], {}, float("nan")
 
     # served: the same arrivals, submitted from a client thread
     srv = Server(hbm_budget=int(budget_gb * (1 << 30)), max_cases=256, steps_per_round=16, device=device)
@@ -285,7 +289,7 @@ def run_serving(n_req, step_scale, device, budget_gb=150.0):
             "hbm_peak_GB": st["hbm_peak"] / 1e9, "rounds": st["rounds"], "graph_builds": st["graph_builds"],
             "gpu_busy_s": st["gpu_busy_s"], "build_s": st["build_s"], "mean_resident": st["mean_resident"],
             "served_s": t_served,
-            "identical_to_serial": bool(same), "compared": len(keep),
+            "identical_to_serial": bool(same) if serial else None, "compared": len(keep),
             "serial": "one Lattice per request in arrival order, one step per call + synchronize "
                       "(the reference driver's launch + queue.finish per step)"}
 
@@ -399,16 +403,51 @@ def force_series(res, samples=20, every=250):
             "note": "after the timed steps, from the channel started at rest (start-up transient)"}
 
 
+def _cpulist(text):
+    out = set()
+    for part in text.strip().split(","):
+        if part:
+            a, _, b = part.partition("-")
+            out.update(range(int(a), int(b or a) + 1))
+    return out
+
+
+def gpu_local_cpus(device):
+    """(NUMA node, host CPUs of that node this process may run on) of the GPU's PCI device, or
+    (None, None) when the system does not say."""
+    import torch
+    try:
+        p = torch.cuda.get_device_properties(device)
+        bus = f"{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+        node = int(open(f"/sys/bus/pci/devices/{bus}/numa_node").read())
+        if node < 0:
+            return None, None
+        cpus = _cpulist(open(f"/sys/devices/system/node/node{node}/cpulist").read()) & os.sched_getaffinity(0)
+        return (node, cpus) if cpus else (None, None)
+    except Exception:
+        return None, None
+
+
 def run_e2e(res, steps, device):
-    """Upload from pinned host memory, E2E_INNER steps, download: timed with CUDA events, the copies inside."""
+    """Upload from pinned host memory, E2E_INNER steps, download: timed with CUDA events, the copies inside.
+    The pinned buffers are allocated from a CPU of the GPU's own NUMA node when the system names one,
+    so that their pages lie in the memory next to the GPU."""
     import torch
     lat, c, sel = res["lat"], res["case"], res["sel"]
     f0 = c.f
     if f0 is None:  # a case started from rest on the device: its host populations are the weights
         from lbffs_gb300 import case as K
         f0 = np.repeat(K.lattice(c.q)[1], c.elements)
-    host_in = torch.from_numpy(f0).pin_memory()
-    host_out = torch.empty_like(host_in).pin_memory()
+    node, cpus = gpu_local_cpus(device)
+    keep_aff = os.sched_getaffinity(0)
+    if cpus:
+        os.sched_setaffinity(0, cpus)
+    try:
+        host_in = torch.from_numpy(f0).pin_memory()
+        host_out = torch.empty_like(host_in).pin_memory()
+        host_out.zero_()  # pages placed by this thread
+    finally:
+        os.sched_setaffinity(0, keep_aff)
     stream = torch.cuda.ExternalStream(lat.stream(), device=device)
     import ctypes as C
     lib = lat.lib
@@ -436,7 +475,7 @@ def run_e2e(res, steps, device):
     mlups = c.elements * E2E_INNER * n_e2e / (ms * 1e-3) / 1e6
     return {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": int(host_in.numel() * 4),
             "d2h_bytes_per_step": int(host_out.numel() * 4), "inner_steps": E2E_INNER, "e2e_steps": n_e2e,
-            "ms_per_e2e_step": ms / n_e2e}
+            "ms_per_e2e_step": ms / n_e2e, "host_numa_node": node}
 
 
 def cpu_reference_mlups(nx, ny, nz, steps, threads=0, kind_pref="reference"):
@@ -478,6 +517,8 @@ def main():
     ap.add_argument("--requests", type=int, default=512, help="serving workload: number of requests")
     ap.add_argument("--step-scale", type=float, default=1.0, help="serving workload: step count scale")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-serial", action="store_true",
+                    help="serving workload: the served run alone, without the serial baselines")
     ap.add_argument("--bulk-kind", type=int, default=0, choices=[0, 1],
                     help="D3Q19 bulk kernel: 0 per-thread loads, 1 row-staged bulk copies")
     ap.add_argument("--profile", action="store_true",
@@ -527,7 +568,7 @@ def main():
 
     if args.workload == "serving":
         if rank == 0:
-            out = run_serving(args.requests, args.step_scale, device)
+            out = run_serving(args.requests, args.step_scale, device, serial=not args.no_serial)
             out.update({"metric": "served solves/s", "unit": "solves/s", "value": out["solves_per_s"],
                         "higher_is_better": True, "n_gpus": 1, "dtype": "f32/fp16s", "data": "synthetic"})
             print(json.dumps(out))

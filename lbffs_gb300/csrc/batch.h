@@ -38,29 +38,27 @@ constexpr int BATCH_TILES_PER_CTA = LBFFS_BATCH_TILES;
 
 // Bulk step of every case in cases[0..ncases), in k_bulk's row tiles (bulk_block) for wide rows and
 // in the segment mapping of bulk_segments (narrow rows keep the lanes busy) for the others: CTA b
-// runs run b - tile_start[c] of the case c
-// with tile_start[c] <= b < tile_start[c + 1] (prefix sums of runs of BATCH_TILES_PER_CTA tiles;
-// ntiles = tile_start[ncases] CTAs).  rows: the launch over the row-tile cases (the others count 0
-// tiles in its prefix sums), else over the segment cases.
-cudaError_t batch_bulk(int storage, bool les, bool rows, const BatchCase* cases, const int* tile_start, int ncases,
-                       int ntiles, const long long* done, cudaStream_t st);
+// runs tiles [BATCH_TILES_PER_CTA y, BATCH_TILES_PER_CTA (y + 1)) of case x, (x, y) = cta_run[b],
+// nctas CTAs.  rows: the launch over the row-tile cases, else over the segment cases.
+cudaError_t batch_bulk(int storage, bool les, bool rows, const BatchCase* cases, const int2* cta_run, int nctas,
+                       const long long* done, cudaStream_t st);
 // Boundary step: thread (warp: warp) t runs entry t - sp_start[c] of case c's special list.
 cudaError_t batch_special(int storage, bool warp, const BatchCase* cases, const long long* sp_start, int ncases,
                           long long nspecial, const long long* done, cudaStream_t st);
-// Ghost layers: CTA b runs ghost-fill block b - h_start[c] of case c's source populations.
-cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nblocks,
+// Ghost layers: CTA b fills ghost block y of case x's source populations, (x, y) = cta_block[b].
+cudaError_t batch_halo(int storage, const BatchCase* cases, const int2* cta_block, long long nblocks,
                        const long long* done, cudaStream_t st);
 // Advance the step counters of the listed slots that have not reached their nsteps.
 cudaError_t batch_tick(const int* slots, const long long* nsteps, int n, long long* done, cudaStream_t st);
 
 // per storage format (batch_inst.cu compiled once per format)
-cudaError_t batch_bulk_s0(bool, bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
-cudaError_t batch_bulk_s1(bool, bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
-cudaError_t batch_bulk_s2(bool, bool, const BatchCase*, const int*, int, int, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s0(bool, bool, const BatchCase*, const int2*, int, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s1(bool, bool, const BatchCase*, const int2*, int, const long long*, cudaStream_t);
+cudaError_t batch_bulk_s2(bool, bool, const BatchCase*, const int2*, int, const long long*, cudaStream_t);
 cudaError_t batch_special_s0(bool, const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
-cudaError_t batch_halo_s0(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
-cudaError_t batch_halo_s1(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
-cudaError_t batch_halo_s2(const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
+cudaError_t batch_halo_s0(const BatchCase*, const int2*, long long, const long long*, cudaStream_t);
+cudaError_t batch_halo_s1(const BatchCase*, const int2*, long long, const long long*, cudaStream_t);
+cudaError_t batch_halo_s2(const BatchCase*, const int2*, long long, const long long*, cudaStream_t);
 cudaError_t batch_special_s1(bool, const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
 cudaError_t batch_special_s2(bool, const BatchCase*, const long long*, int, long long, const long long*, cudaStream_t);
 

@@ -49,36 +49,33 @@ __device__ __forceinline__ int find_case(const T* __restrict__ start, int n, T k
 // two mappings are separate kernels so that each keeps its own register allocation
 template <bool LES, bool ROWS>
 __global__ void LBFFS_BATCH_BOUNDS k_bulk_batch(const BatchCase* __restrict__ cases,
-                                                        const int* __restrict__ tile_start, int ncases,
+                                                        const int2* __restrict__ cta_run,
                                                         const long long* __restrict__ done)
 {
+    // the CTA's case and run of tiles, one read (no search over the case table)
+    const int2 cr = __ldg(cta_run + blockIdx.x);
+    const int c = cr.x, run = cr.y;
 #if LBFFS_BATCH_ARGS_SMEM
     __shared__ StepArgs sa;
-    __shared__ int s_case, s_parity, s_last;
+    __shared__ int s_parity, s_last;
     if (threadIdx.x == 0) {
-        const int c = find_case<int>(tile_start, ncases, (int)blockIdx.x);
         const long long d = done[cases[c].slot];
-        s_case = c;
         s_parity = d < cases[c].nsteps ? (int)(d & 1) : -1;
         s_last = d + 1 == cases[c].nsteps;
     }
     __syncthreads();
     if (s_parity < 0) return;  // the case has finished; it leaves the batch at the next rebuild
-    const int* src = reinterpret_cast<const int*>(&cases[s_case].args[s_parity]);
+    const int* src = reinterpret_cast<const int*>(&cases[c].args[s_parity]);
     int* dst = reinterpret_cast<int*>(&sa);
     for (int w = threadIdx.x; w < (int)(sizeof(StepArgs) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
     __syncthreads();
     if (threadIdx.x == 0 && s_last) sa.store_all = 1;  // full macroscopic fields on the final step
     __syncthreads();
-    const int c = s_case;
 #else
-    // every thread finds the case (the same few cached words): no barrier before the work
-    const int c = find_case<int>(tile_start, ncases, (int)blockIdx.x);
     const long long d = done[cases[c].slot];
     if (d >= cases[c].nsteps) return;  // the case has finished; it leaves the batch at the next rebuild
     const StepArgs& sa = d + 1 == cases[c].nsteps ? cases[c].last : cases[c].args[d & 1];
 #endif
-    const int run = (int)blockIdx.x - tile_start[c];
     const int tiles = cases[c].tiles;
     const int t1 = min(tiles, (run + 1) * BATCH_TILES_PER_CTA);
     if constexpr (ROWS) {
@@ -126,18 +123,19 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch_warp(const BatchCa
 using W = typename std::conditional<S == ST_FP32, uint32_t, uint16_t>::type;
 
 // CTA b runs ghost-fill block b - h_start[c] of case c (h_start: prefix sums of halo blocks)
+// CTA b fills ghost block y of case x, (x, y) = cta_block[b]
 __global__ void __launch_bounds__(HALO_BS) k_halo_batch(const BatchCase* __restrict__ cases,
-                                                        const long long* __restrict__ h_start, int ncases,
+                                                        const int2* __restrict__ cta_block,
                                                         const long long* __restrict__ done)
 {
-    const long long b = blockIdx.x;
-    const int c = find_case<long long>(h_start, ncases, b);
+    const int2 cb = __ldg(cta_block + blockIdx.x);
+    const int c = cb.x;
     const long long d = done[cases[c].slot];
     if (d >= cases[c].nsteps) return;
     const StepArgs& a = cases[c].args[d & 1];
     const PadGeom g{a.nx, a.ny, a.nz, a.px, a.pxy, a.porg, a.pE};
     // the ghosts of this step's source copy (k_bulk / k_special read it only after this launch)
-    halo_block<19, W>(static_cast<W*>(const_cast<void*>(a.f_in)), a.flags, a.bc, g, b - h_start[c], threadIdx.x);
+    halo_block<19, W>(static_cast<W*>(const_cast<void*>(a.f_in)), a.flags, a.bc, g, cb.y, threadIdx.x);
 }
 
 }  // namespace
@@ -145,16 +143,16 @@ __global__ void __launch_bounds__(HALO_BS) k_halo_batch(const BatchCase* __restr
 #define LBFFS_CAT2(a, b) a##b
 #define LBFFS_CAT(a, b) LBFFS_CAT2(a, b)
 
-cudaError_t LBFFS_CAT(batch_bulk_s, LBFFS_S)(bool les, bool rows, const BatchCase* cases, const int* tile_start,
-                                             int ncases, int ntiles, const long long* done, cudaStream_t st)
+cudaError_t LBFFS_CAT(batch_bulk_s, LBFFS_S)(bool les, bool rows, const BatchCase* cases, const int2* cta_run,
+                                             int nctas, const long long* done, cudaStream_t st)
 {
-    if (ntiles <= 0) return cudaSuccess;
+    if (nctas <= 0) return cudaSuccess;
     if (rows) {
-        if (les) k_bulk_batch<true, true><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
-        else k_bulk_batch<false, true><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+        if (les) k_bulk_batch<true, true><<<nctas, BULK_BX, 0, st>>>(cases, cta_run, done);
+        else k_bulk_batch<false, true><<<nctas, BULK_BX, 0, st>>>(cases, cta_run, done);
     } else {
-        if (les) k_bulk_batch<true, false><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
-        else k_bulk_batch<false, false><<<ntiles, BULK_BX, 0, st>>>(cases, tile_start, ncases, done);
+        if (les) k_bulk_batch<true, false><<<nctas, BULK_BX, 0, st>>>(cases, cta_run, done);
+        else k_bulk_batch<false, false><<<nctas, BULK_BX, 0, st>>>(cases, cta_run, done);
     }
     return cudaGetLastError();
 }
@@ -175,11 +173,11 @@ cudaError_t LBFFS_CAT(batch_special_s, LBFFS_S)(bool warp, const BatchCase* case
     return cudaGetLastError();
 }
 
-cudaError_t LBFFS_CAT(batch_halo_s, LBFFS_S)(const BatchCase* cases, const long long* h_start, int ncases,
+cudaError_t LBFFS_CAT(batch_halo_s, LBFFS_S)(const BatchCase* cases, const int2* cta_block,
                                              long long nblocks, const long long* done, cudaStream_t st)
 {
     if (nblocks <= 0) return cudaSuccess;
-    k_halo_batch<<<(unsigned)nblocks, HALO_BS, 0, st>>>(cases, h_start, ncases, done);
+    k_halo_batch<<<(unsigned)nblocks, HALO_BS, 0, st>>>(cases, cta_block, done);
     return cudaGetLastError();
 }
 

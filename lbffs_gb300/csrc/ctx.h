@@ -15,6 +15,12 @@ namespace lbffs {
 struct OutputState;  // output.cu: fields of lbffs_output and the asynchronous file writer
 }
 
+// host <-> device copies of FP32 populations in flight at once (one direction plane per copy); a
+// build-time tuning value
+#ifndef LBFFS_COPY_STREAMS
+#define LBFFS_COPY_STREAMS 4
+#endif
+
 struct lbffs_ctx {
     lbffs_desc d{};
     int Q = 19;
@@ -45,8 +51,8 @@ struct lbffs_ctx {
     // pulls across the grid's border: face_ok when every face carries one boundary code per axis
     // (face_codes, StepArgs layout) and the face flag is set on exactly the border cells; pull_ok
     // when moreover both x faces carry boundary-kernel codes (inlet / outlet / fixed density / wall
-    // function), so bulk rows cross only y / z faces: a single-lattice context then runs without a
-    // ghost layer
+    // function), so bulk rows cross only y / z faces: the context (alone or served) then runs
+    // without a ghost layer
     int face_codes = 0;
     bool face_ok = false;
     bool pull_ok = false;
@@ -73,6 +79,10 @@ struct lbffs_ctx {
     // the boundary kernel runs beside the bulk kernel on a second stream (lbffs_step)
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    // FP32 population transfers: the direction planes' copies spread over these streams (created on
+    // the first transfer), with one event each to join them back into the context's stream
+    cudaStream_t copy_st[LBFFS_COPY_STREAMS] = {};
+    cudaEvent_t copy_ev[LBFFS_COPY_STREAMS + 1] = {};
 
     // output step and asynchronous writes (output.cu)
     lbffs::OutputState* out = nullptr;

@@ -159,6 +159,10 @@ extern "C" int lbffs_destroy(lbffs_ctx* c)
     }
     for (auto e : c->pool) cudaEventDestroy(e);
     if (c->side) cudaStreamDestroy(c->side);
+    for (auto s : c->copy_st)
+        if (s) cudaStreamDestroy(s);
+    for (auto e : c->copy_ev)
+        if (e) cudaEventDestroy(e);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);
@@ -393,7 +397,7 @@ static int commit(lbffs_ctx* c)
         auto kernel_face = [](int code) {
             return code == BC_OUTLET || code == BC_FIXVEL || code == BC_FIXDEN || code == BC_WALLFN;
         };
-        c->pull_ok = LBFFS_BORDER_PULLS && c->face_ok && c->arena == nullptr && kernel_face(c->face_codes & 7) &&
+        c->pull_ok = LBFFS_BORDER_PULLS && c->face_ok && kernel_face(c->face_codes & 7) &&
                      kernel_face((c->face_codes >> 3) & 7);
     }
     // uniform relaxation rate: the value at the domain centre
@@ -437,7 +441,7 @@ static int commit(lbffs_ctx* c)
 // Population q of an FP32 context between the reference's dense host layout (f[q * E + ic]) and
 // the padded device planes of the current copy (upload: into copy 0), as one pitched 3-D copy:
 // rows of nx floats, the device rows px apart and its planes pxy apart.
-static cudaError_t copy_plane_f32(lbffs_ctx* c, int q, const float* host_in, bool upload)
+static cudaError_t copy_plane_f32(lbffs_ctx* c, int q, const float* host_in, bool upload, cudaStream_t st)
 {
     const PadGeom& g = c->pg;
     float* dev = static_cast<float*>(upload ? c->f[0] : c->f[c->fcur]) + (size_t)q * (size_t)g.pE + g.porg;
@@ -449,7 +453,36 @@ static cudaError_t copy_plane_f32(lbffs_ctx* c, int q, const float* host_in, boo
     p.dstPtr = upload ? dp : hp;
     p.extent = make_cudaExtent((size_t)g.nx * sizeof(float), (size_t)g.ny, (size_t)g.nz);
     p.kind = upload ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
-    return cudaMemcpy3DAsync(&p, c->stream);
+    return cudaMemcpy3DAsync(&p, st);
+}
+
+// The Q plane copies of an FP32 population transfer, LBFFS_COPY_STREAMS of them in flight at once
+// (each copy engine moves one pitched copy at a time), ordered after and joined back into the
+// context's stream.
+static cudaError_t copy_planes_f32(lbffs_ctx* c, const float* host, bool upload)
+{
+    cudaError_t e = cudaSuccess;
+    if (LBFFS_COPY_STREAMS > 1 && !c->copy_st[0]) {
+        for (int k = 0; k < LBFFS_COPY_STREAMS && e == cudaSuccess; k++)
+            e = cudaStreamCreateWithFlags(&c->copy_st[k], cudaStreamNonBlocking);
+        for (int k = 0; k <= LBFFS_COPY_STREAMS && e == cudaSuccess; k++)
+            e = cudaEventCreateWithFlags(&c->copy_ev[k], cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
+    if (LBFFS_COPY_STREAMS <= 1) {
+        for (int q = 0; q < c->Q && e == cudaSuccess; q++) e = copy_plane_f32(c, q, host, upload, c->stream);
+        return e;
+    }
+    e = cudaEventRecord(c->copy_ev[LBFFS_COPY_STREAMS], c->stream);
+    for (int k = 0; k < LBFFS_COPY_STREAMS && e == cudaSuccess; k++)
+        e = cudaStreamWaitEvent(c->copy_st[k], c->copy_ev[LBFFS_COPY_STREAMS], 0);
+    for (int q = 0; q < c->Q && e == cudaSuccess; q++)
+        e = copy_plane_f32(c, q, host, upload, c->copy_st[q % LBFFS_COPY_STREAMS]);
+    for (int k = 0; k < LBFFS_COPY_STREAMS && e == cudaSuccess; k++) {
+        e = cudaEventRecord(c->copy_ev[k], c->copy_st[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->copy_ev[k], 0);
+    }
+    return e;
 }
 
 extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t bytes)
@@ -474,7 +507,7 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
         if (c->d.storage == LBFFS_FP32) {
             // FP32 is stored as is: one pitched copy per direction into the padded planes, then the
             // second copy device to device (no staging, no conversion kernel)
-            for (int q = 0; q < c->Q; q++) CK(copy_plane_f32(c, q, h, true));
+            CK(copy_planes_f32(c, h, true));
             CK(cudaMemcpyAsync(c->f[1], c->f[0], (size_t)c->Q * (size_t)c->pg.pE * sizeof(float),
                                cudaMemcpyDeviceToDevice, c->stream));
             CK(cudaStreamSynchronize(c->stream));
@@ -519,7 +552,7 @@ extern "C" int lbffs_download(lbffs_ctx* c, int field, void* host, size_t bytes)
         const long long rows = (long long)c->Q * c->d.ny * c->d.nz, chunk = (long long)c->stage_elems / nx;
         float* h = static_cast<float*>(host);
         if (c->d.storage == LBFFS_FP32) {
-            for (int q = 0; q < c->Q; q++) CK(copy_plane_f32(c, q, h, false));
+            CK(copy_planes_f32(c, h, false));
             CK(cudaStreamSynchronize(c->stream));
             return LBFFS_OK;
         }

@@ -64,9 +64,9 @@ struct Group {
     bool les = false;
     std::vector<Request*> members;
     BatchCase* d_cases = nullptr;
-    int* d_tiles = nullptr;  // prefix sums of bulk CTAs: segment cases [0, n], then row-tile cases
+    int2* d_ctas = nullptr;  // (case, run) of each bulk CTA: the segment launch's, then the row-tile launch's
+    size_t ctas_cap = 0;
     long long* d_sp = nullptr;
-    long long* d_halo = nullptr;
     size_t cap = 0;
     int ntiles = 0, ntiles_rows = 0;
     long long nspecial = 0, nhalo = 0;
@@ -276,8 +276,8 @@ cudaError_t build_batch(lbffs_server* s)
             continue;
         }
         std::vector<BatchCase> hc(n);
-        std::vector<int> tiles(2 * (n + 1), 0);  // segment cases, then row-tile cases
-        std::vector<long long> sp(n + 1, 0), hl(n + 1, 0);
+        std::vector<int2> seg_ctas, row_ctas, halo_ctas;
+        std::vector<long long> sp(n + 1, 0);
         for (int i = 0; i < n; i++) {
             Request* r = g.members[i];
             r->in_graph = true;
@@ -287,6 +287,7 @@ cudaError_t build_batch(lbffs_server* s)
                 // the resident cases together exceed L2, whatever one case's size: no policy
                 // (evict-first measured 3 % slower on the served sample)
                 hc[i].args[p].l2_policy = 0;
+                hc[i].args[p].border_pulls = c->pull_ok && c->n_markers <= 1 ? 1 : 0;
             }
             hc[i].last = hc[i].args[(r->nsteps - 1) & 1];
             hc[i].last.store_all = 1;
@@ -303,37 +304,43 @@ cudaError_t build_batch(lbffs_server* s)
                                         : (int)(((long long)hc[i].seg_per_row * c->d.ny * c->d.nz +
                                                  BATCH_SEG_PER_TILE - 1) / BATCH_SEG_PER_TILE);
             const int ctas = (hc[i].tiles + BATCH_TILES_PER_CTA - 1) / BATCH_TILES_PER_CTA;
-            tiles[i + 1] = tiles[i] + (hc[i].rowtile ? 0 : ctas);
-            tiles[n + 2 + i] = tiles[n + 1 + i] + (hc[i].rowtile ? ctas : 0);
+            for (int r = 0; r < ctas; r++) (hc[i].rowtile ? row_ctas : seg_ctas).push_back(make_int2(i, r));
+            // a case whose x faces are boundary-kernel faces pulls across its border (no ghost fill)
+            if (!hc[i].args[0].border_pulls) {
+                const long long hb = halo_blocks(c->pg, 19, 0) + halo_blocks(c->pg, 19, 1) + halo_blocks(c->pg, 19, 2);
+                for (long long b = 0; b < hb; b++) halo_ctas.push_back(make_int2(i, (int)b));
+            }
             sp[i + 1] = sp[i] + c->n_special;
-            hl[i + 1] = hl[i] + halo_blocks(c->pg, 19, 0) + halo_blocks(c->pg, 19, 1) + halo_blocks(c->pg, 19, 2);
         }
         size_t cap = g.cap;
         if (n + 1 > (int)g.cap || !g.d_cases) {
             if (g.d_cases) cudaFree(g.d_cases);
-            if (g.d_tiles) cudaFree(g.d_tiles);
             if (g.d_sp) cudaFree(g.d_sp);
-            if (g.d_halo) cudaFree(g.d_halo);
             cap = (size_t)(n + 1) * 2;
             if ((e = cudaMalloc(&g.d_cases, sizeof(BatchCase) * cap)) != cudaSuccess) return e;
-            if ((e = cudaMalloc(&g.d_tiles, sizeof(int) * 2 * cap)) != cudaSuccess) return e;
             if ((e = cudaMalloc(&g.d_sp, sizeof(long long) * cap)) != cudaSuccess) return e;
-            if ((e = cudaMalloc(&g.d_halo, sizeof(long long) * cap)) != cudaSuccess) return e;
             g.cap = cap;
         }
         if ((e = cudaMemcpyAsync(g.d_cases, hc.data(), sizeof(BatchCase) * n, cudaMemcpyHostToDevice, s->stream)))
             return e;
-        if ((e = cudaMemcpyAsync(g.d_tiles, tiles.data(), sizeof(int) * 2 * (n + 1), cudaMemcpyHostToDevice,
-                                 s->stream)))
+        const size_t nctas = seg_ctas.size() + row_ctas.size() + halo_ctas.size();
+        if (nctas > g.ctas_cap || !g.d_ctas) {
+            if (g.d_ctas) cudaFree(g.d_ctas);
+            g.d_ctas = nullptr;
+            g.ctas_cap = nctas * 2 + 64;
+            if ((e = cudaMalloc(&g.d_ctas, sizeof(int2) * g.ctas_cap)) != cudaSuccess) return e;
+        }
+        const size_t nseg = seg_ctas.size(), nrow = row_ctas.size();
+        seg_ctas.insert(seg_ctas.end(), row_ctas.begin(), row_ctas.end());
+        seg_ctas.insert(seg_ctas.end(), halo_ctas.begin(), halo_ctas.end());
+        if ((e = cudaMemcpyAsync(g.d_ctas, seg_ctas.data(), sizeof(int2) * nctas, cudaMemcpyHostToDevice, s->stream)))
             return e;
         if ((e = cudaMemcpyAsync(g.d_sp, sp.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, s->stream)))
             return e;
-        if ((e = cudaMemcpyAsync(g.d_halo, hl.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, s->stream)))
-            return e;
-        g.ntiles = tiles[n];
-        g.ntiles_rows = tiles[2 * n + 1];
+        g.ntiles = (int)nseg;
+        g.ntiles_rows = (int)nrow;
         g.nspecial = sp[n];
-        g.nhalo = hl[n];
+        g.nhalo = (long long)halo_ctas.size();
     }
     std::vector<int> slots;
     std::vector<long long> ns;
@@ -361,7 +368,8 @@ cudaError_t build_batch(lbffs_server* s)
     for (int step = 0; step < s->d.steps_per_round && le == cudaSuccess; step++) {
         for (Group& g : s->groups)
             if (le == cudaSuccess && g.nhalo > 0)
-                le = batch_halo(g.storage, g.d_cases, g.d_halo, (int)g.members.size(), g.nhalo, s->d_done, s->stream);
+                le = batch_halo(g.storage, g.d_cases, g.d_ctas + g.ntiles + g.ntiles_rows, g.nhalo, s->d_done,
+                                s->stream);
         // the boundary kernels write other cells than the bulk kernels and read the same source
         // copy: a parallel branch of the graph, joined before the counter tick
         if (le == cudaSuccess && any_special) {
@@ -374,12 +382,11 @@ cudaError_t build_batch(lbffs_server* s)
             if (le == cudaSuccess) le = cudaEventRecord(s->join_ev, s->branch);
         }
         for (Group& g : s->groups) {
-            const int n = (int)g.members.size();
             if (le == cudaSuccess && g.ntiles_rows > 0)
-                le = batch_bulk(g.storage, g.les, true, g.d_cases, g.d_tiles + n + 1, n, g.ntiles_rows, s->d_done,
+                le = batch_bulk(g.storage, g.les, true, g.d_cases, g.d_ctas + g.ntiles, g.ntiles_rows, s->d_done,
                                 s->stream);
             if (le == cudaSuccess && g.ntiles > 0)
-                le = batch_bulk(g.storage, g.les, false, g.d_cases, g.d_tiles, n, g.ntiles, s->d_done, s->stream);
+                le = batch_bulk(g.storage, g.les, false, g.d_cases, g.d_ctas, g.ntiles, s->d_done, s->stream);
         }
         if (le == cudaSuccess && any_special) le = cudaStreamWaitEvent(s->stream, s->join_ev, 0);
         if (le == cudaSuccess) le = batch_tick(s->d_tick_slots, s->d_tick_nsteps, s->ntick, s->d_done, s->stream);
@@ -569,24 +576,24 @@ cudaError_t batch_tick(const int* slots, const long long* nsteps, int n, long lo
     return cudaGetLastError();
 }
 
-cudaError_t batch_bulk(int storage, bool les, bool rows, const BatchCase* cases, const int* tile_start, int ncases,
-                       int ntiles, const long long* done, cudaStream_t st)
+cudaError_t batch_bulk(int storage, bool les, bool rows, const BatchCase* cases, const int2* cta_run, int nctas,
+                       const long long* done, cudaStream_t st)
 {
     switch (storage) {
-        case ST_FP32: return batch_bulk_s0(les, rows, cases, tile_start, ncases, ntiles, done, st);
-        case ST_FP16S: return batch_bulk_s1(les, rows, cases, tile_start, ncases, ntiles, done, st);
-        case ST_BF16S: return batch_bulk_s2(les, rows, cases, tile_start, ncases, ntiles, done, st);
+        case ST_FP32: return batch_bulk_s0(les, rows, cases, cta_run, nctas, done, st);
+        case ST_FP16S: return batch_bulk_s1(les, rows, cases, cta_run, nctas, done, st);
+        case ST_BF16S: return batch_bulk_s2(les, rows, cases, cta_run, nctas, done, st);
     }
     return cudaErrorInvalidValue;
 }
 
-cudaError_t batch_halo(int storage, const BatchCase* cases, const long long* h_start, int ncases, long long nblocks,
+cudaError_t batch_halo(int storage, const BatchCase* cases, const int2* cta_block, long long nblocks,
                        const long long* done, cudaStream_t st)
 {
     switch (storage) {
-        case ST_FP32: return batch_halo_s0(cases, h_start, ncases, nblocks, done, st);
-        case ST_FP16S: return batch_halo_s1(cases, h_start, ncases, nblocks, done, st);
-        case ST_BF16S: return batch_halo_s2(cases, h_start, ncases, nblocks, done, st);
+        case ST_FP32: return batch_halo_s0(cases, cta_block, nblocks, done, st);
+        case ST_FP16S: return batch_halo_s1(cases, cta_block, nblocks, done, st);
+        case ST_BF16S: return batch_halo_s2(cases, cta_block, nblocks, done, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -666,9 +673,8 @@ extern "C" int lbffs_server_destroy(lbffs_server* s)
     if (s->exec) cudaGraphExecDestroy(s->exec);
     for (Group& g : s->groups) {
         if (g.d_cases) cudaFree(g.d_cases);
-        if (g.d_tiles) cudaFree(g.d_tiles);
+        if (g.d_ctas) cudaFree(g.d_ctas);
         if (g.d_sp) cudaFree(g.d_sp);
-        if (g.d_halo) cudaFree(g.d_halo);
     }
     if (s->d_tick_slots) cudaFree(s->d_tick_slots);
     if (s->d_tick_nsteps) cudaFree(s->d_tick_nsteps);
