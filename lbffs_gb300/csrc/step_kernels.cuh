@@ -104,15 +104,18 @@ __device__ __forceinline__ float smagorinsky(const float (&ft)[Q], float rho, fl
 // y+ from the log law u+ = ln(E y+) / kappa at wall distance y with the cell's own speed, by the
 // fixed-point iteration y+ <- (kappa |u| y / nu + y+) / (1 + ln(E y+)) from y+ = 1 (at most 10 times,
 // until y+ moves by at most 0.001); kappa 0.41, A+ 26, E 9.8, nu = (tau - 1/2) / 3.  1 + 1e-10 is 1 in
-// FP32, as in the reference's float expression.
-static __device__ __noinline__ float van_driest_ratio(float y, float umag, float nu, float cs)
+// FP32, as in the reference's float expression.  The iteration runs on the hardware logarithm and
+// an approximate division (a few ulp per step of a contraction whose result is used to 1e-3); the
+// loop-invariant kappa |u| y / nu is formed once.
+static __device__ __forceinline__ float van_driest_ratio(float y, float umag, float nu, float cs)
 {
     const float kappa = 0.41f, Aplus = 26.f, Ek = 9.8f;
+    const float a = kappa * umag * y / nu;
     float yp = 1.f, ypn;
     int it = 0;
     do {
         ypn = yp;
-        yp = (kappa * umag * y / nu + yp) / (1.f + logf(Ek * yp));
+        yp = __fdividef(a + yp, 1.f + __logf(Ek * yp));
         it++;
     } while (fabsf(yp - ypn) > 0.001f && it < 10);
     return (kappa / cs) * (1.f - expf(-yp / Aplus)) * y;
