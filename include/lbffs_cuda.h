@@ -195,8 +195,8 @@ int lbffs_cell_counts(lbffs_ctx* ctx, long long out[4]);
 int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
 
 /* No counterpart in the reference (a choice between two mappings of the same boundary kernel,
-   which give identical results).  kind 0: one thread per cell of the special list; kind 1: one warp
-   per cell, lane q doing direction q's reads; -1 (the default): kind 1 for lists of at most
+   which give identical results).  kind 0: one thread per cell of the special list; kind 1: a group
+   of 16 lanes per cell, lane g doing the reads of directions g and g + 16; -1 (the default): kind 1 for lists of at most
    LBFFS_SPECIAL_WARP_MAX cells, where one thread per cell leaves most SMs idle, else kind 0.
    D3Q27 contexts always use kind 0. */
 #define LBFFS_SPECIAL_WARP_MAX 16384

@@ -255,8 +255,8 @@ class Lattice:
         self._check(self.lib.lbffs_set_bulk_kernel(self.h, int(kind)))
 
     def set_special_kernel(self, kind):
-        """Boundary kernel mapping: 0 one thread per listed cell, 1 one warp per cell, -1 by the list's
-        length (same results)."""
+        """Boundary kernel mapping: 0 one thread per listed cell, 1 a lane group per cell, -1 by the
+        list's length (same results)."""
         self._check(self.lib.lbffs_set_special_kernel(self.h, int(kind)))
 
     def init_rest(self):

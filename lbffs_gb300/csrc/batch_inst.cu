@@ -107,17 +107,18 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch(const BatchCase* _
     special_cell<19, S, COLL_RR>(cases[c].args[d & 1], t - sp_start[c]);
 }
 
-// one warp per listed cell (special_cell with WARP), for short lists
+// a group of LBFFS_SPECIAL_LANES lanes per listed cell (special_cell with G lanes), for short lists
 __global__ void __launch_bounds__(SPECIAL_BS) k_special_batch_warp(const BatchCase* __restrict__ cases,
                                                                    const long long* __restrict__ sp_start,
                                                                    int ncases, const long long* __restrict__ done)
 {
-    const long long t = (long long)blockIdx.x * (SPECIAL_BS / 32) + (threadIdx.x >> 5);
+    constexpr int G = LBFFS_SPECIAL_LANES;
+    const long long t = (long long)blockIdx.x * (SPECIAL_BS / G) + (threadIdx.x / G);
     if (t >= sp_start[ncases]) return;
     const int c = find_case<long long>(sp_start, ncases, t);
     const long long d = done[cases[c].slot];
     if (d >= cases[c].nsteps) return;
-    special_cell<19, S, COLL_RR, true>(cases[c].args[d & 1], t - sp_start[c]);
+    special_cell<19, S, COLL_RR, LBFFS_SPECIAL_LANES>(cases[c].args[d & 1], t - sp_start[c]);
 }
 
 using W = typename std::conditional<S == ST_FP32, uint32_t, uint16_t>::type;
@@ -163,7 +164,7 @@ cudaError_t LBFFS_CAT(batch_special_s, LBFFS_S)(bool warp, const BatchCase* case
 {
     if (nspecial <= 0) return cudaSuccess;
     if (warp) {
-        constexpr int per = SPECIAL_BS / 32;
+        constexpr int per = SPECIAL_BS / LBFFS_SPECIAL_LANES;
         k_special_batch_warp<<<(unsigned)((nspecial + per - 1) / per), SPECIAL_BS, 0, st>>>(cases, sp_start, ncases,
                                                                                             done);
         return cudaGetLastError();

@@ -77,7 +77,8 @@ struct lbffs_ctx {
     bool own_stream = true, own_stage = true;
 
     // the boundary kernel runs beside the bulk kernel on a second stream (lbffs_step)
-    cudaStream_t side = nullptr;
+    cudaStream_t side = nullptr;     // boundary kernel, one thread per cell: launched first, higher priority
+    cudaStream_t side_lo = nullptr;  // boundary kernel, a lane group per cell: launched after the bulk kernel
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     // FP32 population transfers: the direction planes' copies spread over these streams (created on
     // the first transfer), with one event each to join them back into the context's stream

@@ -217,7 +217,7 @@ struct StepArgs {
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity
     int store_all;    // store rho/u/v/w/tau for every fluid cell this step
     int bulk_kind;    // D3Q19 bulk kernel: 0 per-thread loads, 1 row-staged bulk copies (launch choice)
-    int special_kind;  // boundary kernel: 0 one thread per listed cell, 1 one warp per cell (launch choice)
+    int special_kind;  // boundary kernel: 0 one thread per listed cell, 1 a lane group per cell (launch choice)
     int l2_policy;    // L2 policy of the 2-byte bulk pairs' accesses: 0 none, 1 evict-first (2 evict-normal)
     int sgs, wall;    // Sgs / Wall selections (runtime in the boundary kernel)
     const int* ibm_box;  // device int[6] lo/hi of the marker box (cells inside store macroscopics), or null

@@ -21,7 +21,7 @@ cudaError_t LBFFS_NAME(LBFFS_Q, LBFFS_S, LBFFS_C, LBFFS_PART)(const StepArgs& a,
     if (a.n_special <= 0) return cudaSuccess;
 #if LBFFS_Q == 19
     if (a.special_kind == 1) {
-        constexpr int per = SPECIAL_BS / 32;
+        constexpr int per = SPECIAL_BS / LBFFS_SPECIAL_LANES;
         const dim3 grid((unsigned)((a.n_special + per - 1) / per));
         k_special_warp<LBFFS_Q, LBFFS_S, LBFFS_C><<<grid, SPECIAL_BS, 0, st>>>(a);
         return cudaGetLastError();

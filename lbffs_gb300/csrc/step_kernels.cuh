@@ -1124,7 +1124,7 @@ __global__ void LBFFS_BULK_BOUNDS(Q, LES) k_bulk(const StepArgs a)
     bulk_block<Q, S, COLL, SGS, LES>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
-// ---- one warp per boundary cell (special_cell with WARP) ----
+// ---- a lane group per boundary cell (special_cell with G lanes) ----
 // Lane q < Q of the warp does the per-direction memory work of direction q: its pull, its own
 // previous value, the outlet's inner value and the STL link's reads, all issued in one round trip
 // after the cell index; the values are exchanged by shuffles and the operators run on the full
@@ -1196,12 +1196,16 @@ __device__ __forceinline__ long long border_pull_c(const StepArgs& a, const Bord
     return (long long)m * a.pE + ip;
 }
 
-// The general boundary path of entry t of the special list: one thread per cell, or (WARP) one
-// warp per cell, every lane calling with the same t.
-template <int Q, int S, int COLL, bool WARP = false>
+// The general boundary path of entry t of the special list: one thread per cell (G = 1), or a group
+// of G lanes per cell (G = 8, 16 or 32, aligned within the warp), every lane of the group calling
+// with the same t; lane g of the group does the reads of directions g, g + G, ...
+template <int Q, int S, int COLL, int G = 1>
 __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
 {
     using T = typename Codec<S>::T;
+    constexpr bool GRP = G > 1;
+    constexpr int K = GRP ? (Q + G - 1) / G : 1;  // directions per lane
+    static_assert(G == 1 || G == 8 || G == 16 || G == 32, "lanes per cell");
     const long long ic = a.special[t];
     const int N[3] = {a.nx, a.ny, a.nz};
     const long long nxny = (long long)a.nx * a.ny;
@@ -1230,95 +1234,115 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     // streaming: upwind value, or the face rule's value (upwindID_B + reflectOrMirrorQ): from the
     // ghost that holds it (filled by k_halo), or, with border pulls, read where the rule takes it
     float ft[Q];
-    [[maybe_unused]] const int lane = threadIdx.x & 31;
-    [[maybe_unused]] const int lq = lane < Q ? lane : 0;  // lanes >= Q stand in for direction 0
-    [[maybe_unused]] LaneDir<Q> ld;
-    // WARP: this lane's outlet value and STL-link result with its momentum-exchange sum fb + f_q
-    // (lanes 1..Q-1)
-    [[maybe_unused]] float v_out = 0.f, v_link = 0.f, v_fw = 0.f;
-    [[maybe_unused]] bool has_out = false, link = false;
-    if constexpr (WARP) {
-        ld = lane_dir<Q>(lq);
+    [[maybe_unused]] const int lane = GRP ? (int)(threadIdx.x & (G - 1)) : 0;
+    [[maybe_unused]] const unsigned gmask =
+        G == 32 ? 0xffffffffu : (((1u << (G & 31)) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    [[maybe_unused]] LaneDir<Q> ld[K];
+    // groups: this lane's outlet values and STL-link results with their momentum-exchange sums
+    // fb + f_q, for its directions lane + G k (the rest direction and q >= Q have none)
+    [[maybe_unused]] float v_out[K], v_link[K], v_fw[K];
+    [[maybe_unused]] bool has_out[K], link[K];
+    if constexpr (GRP) {
         const T* fin = static_cast<const T*>(a.f_in);
-        long long el;
-        if (a.border_pulls && (x[0] == 0 || x[0] == N[0] - 1 || x[1] == 0 || x[1] == N[1] - 1 || x[2] == 0 ||
-                               x[2] == N[2] - 1)) {
-            const BorderCell g = border_cell(a, x[0], x[1], x[2]);
-            int m = 0;
+        const bool border = a.border_pulls && (x[0] == 0 || x[0] == N[0] - 1 || x[1] == 0 || x[1] == N[1] - 1 ||
+                                               x[2] == 0 || x[2] == N[2] - 1);
+        const BorderCell g = border_cell(a, x[0], x[1], x[2]);
+        const bool nei = a.nei_solid[ic] == 1;
+        const bool outlet = face && (b[0] == BC_OUTLET || b[1] == BC_OUTLET || b[2] == BC_OUTLET);
+        float fs[K], fo[K], f_in_cell[K], fb[K], sdf1[K], ufc[K][3];
+        int out_axis[K];
 #pragma unroll
-            for (int p = 0; p < Q; p++)
-                if (lq == p) m = missing_dir<Q>(p, g.b);
-            el = border_pull_c(a, g, ld.c, lq, m, ip);
-        } else {
-            el = (long long)lq * a.pE + (ip - (ld.c[0] + ld.c[1] * a.px + ld.c[2] * a.pxy));
-        }
-        const float fs = Codec<S>::load(fin + el, ld.w);
-        const float fo = Codec<S>::load(fin + (long long)lq * a.pE + ip, ld.w);  // the cell's own previous f_q
-        // outflowBC's inner value (the last outlet face of the cell whose inward direction q is)
-        float f_in_cell = 0.f;
-        int out_axis = 0;
-        if (face && (b[0] == BC_OUTLET || b[1] == BC_OUTLET || b[2] == BC_OUTLET)) {
+        for (int k = 0; k < K; k++) {
+            const int qk = lane + G * k;
+            const bool okq = qk < Q;
+            const int lq = okq ? qk : 0;  // lanes past Q stand in for direction 0
+            ld[k] = lane_dir<Q>(lq);
+            long long el;
+            if (border) {
+                int m = 0;
 #pragma unroll
-            for (int d = 0; d < 3; d++) {
-                if (b[d] != BC_OUTLET) continue;
+                for (int p = 0; p < Q; p++)
+                    if (lq == p) m = missing_dir<Q>(p, g.b);
+                el = border_pull_c(a, g, ld[k].c, lq, m, ip);
+            } else {
+                el = (long long)lq * a.pE + (ip - (ld[k].c[0] + ld[k].c[1] * a.px + ld[k].c[2] * a.pxy));
+            }
+            fs[k] = Codec<S>::load(fin + el, ld[k].w);
+            fo[k] = Codec<S>::load(fin + (long long)lq * a.pE + ip, ld[k].w);  // the cell's own previous f_q
+            // outflowBC's inner value (the last outlet face of the cell whose inward direction q is)
+            f_in_cell[k] = 0.f;
+            out_axis[k] = 0;
+            has_out[k] = false;
+            if (outlet) {
 #pragma unroll
-                for (int side = -1; side <= 1; side += 2) {
-                    if (!((side < 0 && x[d] == 0) || (side > 0 && x[d] == N[d] - 1))) continue;
-                    if (lane >= 1 && lane < Q && ld.c[d] == -side) {
-                        f_in_cell = Codec<S>::load(fin + (long long)lq * a.pE + inner_p(d, side), ld.w);
-                        has_out = true;
-                        out_axis = d;
+                for (int d = 0; d < 3; d++) {
+                    if (b[d] != BC_OUTLET) continue;
+#pragma unroll
+                    for (int side = -1; side <= 1; side += 2) {
+                        if (!((side < 0 && x[d] == 0) || (side > 0 && x[d] == N[d] - 1))) continue;
+                        if (qk >= 1 && okq && ld[k].c[d] == -side) {
+                            f_in_cell[k] = Codec<S>::load(fin + (long long)lq * a.pE + inner_p(d, side), ld[k].w);
+                            has_out[k] = true;
+                            out_axis[k] = d;
+                        }
                     }
                 }
             }
-        }
-        // STL link of direction q (internalWallBC): its reads, before the link test resolves
-        const bool nei = a.nei_solid[ic] == 1;
-        float fb = 0.f, sdf1 = 0.f, ufc[3] = {0.f, 0.f, 0.f};
-        if (nei && lane >= 1 && lane < Q) {
-            const long long up = upwind_c(ld.c, x, N, b, face);
-            link = up >= 0 && a.solid[up] == 1;
-            // F(opposite of q, ip); opposite directions have equal weights
-            fb = Codec<S>::load(fin + (long long)ld.opp * a.pE + ip, ld.w);
-            if (a.wall != WALL_BB) {
-                sdf1 = up >= 0 ? a.sdf[up] : 0.f;
-                const int cb[3] = {-ld.c[0], -ld.c[1], -ld.c[2]};
-                const long long fl = upwind_c(cb, x, N, b, face);
-                const long long fc = fl < 0 ? ic : fl;
-                ufc[0] = a.u_p[fc];
-                ufc[1] = a.v_p[fc];
-                ufc[2] = a.w_p[fc];
+            // STL link of direction q (internalWallBC): its reads, before the link test resolves
+            link[k] = false;
+            fb[k] = sdf1[k] = 0.f;
+            ufc[k][0] = ufc[k][1] = ufc[k][2] = 0.f;
+            if (nei && qk >= 1 && okq) {
+                const long long up = upwind_c(ld[k].c, x, N, b, face);
+                link[k] = up >= 0 && a.solid[up] == 1;
+                // F(opposite of q, ip); opposite directions have equal weights
+                fb[k] = Codec<S>::load(fin + (long long)ld[k].opp * a.pE + ip, ld[k].w);
+                if (a.wall != WALL_BB) {
+                    sdf1[k] = up >= 0 ? a.sdf[up] : 0.f;
+                    const int cb[3] = {-ld[k].c[0], -ld[k].c[1], -ld[k].c[2]};
+                    const long long fl = upwind_c(cb, x, N, b, face);
+                    const long long fc = fl < 0 ? ic : fl;
+                    ufc[k][0] = a.u_p[fc];
+                    ufc[k][1] = a.v_p[fc];
+                    ufc[k][2] = a.w_p[fc];
+                }
             }
         }
 #pragma unroll
-        for (int q = 0; q < Q; q++) ft[q] = __shfl_sync(0xffffffffu, fs, q);
+        for (int q = 0; q < Q; q++) ft[q] = __shfl_sync(gmask, fs[q / G], q % G, G);
         const float uo_[3] = {a.u_p[ic], a.v_p[ic], a.w_p[ic]};
-        if (has_out) {
-            const float g = 0.57735026919f - (out_axis == 0 ? uo_[0] : out_axis == 1 ? uo_[1] : uo_[2]);
-            v_out = g * f_in_cell + (1.f - g) * fo;
-        }
-        if (link) {
-            if (a.wall == WALL_BB) {
-                v_link = fb;
-            } else {
-                const float omega_l = a.omega[ic], rho_o = a.rho_p[ic], tau_o = a.tau_p[ic];
-                const float usq = uo_[0] * uo_[0] + uo_[1] * uo_[1] + uo_[2] * uo_[2];
-                const float sdf0 = a.sdf[ic];
-                const float qf = fabsf(sdf0) / (fabsf(sdf0) + fabsf(sdf1));
-                const float we = 1.f / (1.f / omega_l + tau_o);
-                const float uc = -uo_[0] * (float)ld.c[0] - uo_[1] * (float)ld.c[1] - uo_[2] * (float)ld.c[2];
-                float feq, chi;
-                if (qf <= 0.5f) {
-                    const float uf = -ufc[0] * (float)ld.c[0] - ufc[1] * (float)ld.c[1] - ufc[2] * (float)ld.c[2];
-                    feq = (rho_o + 3.f * uf + 4.5f * uc * uc - 1.5f * usq) * ld.w;
-                    chi = we * (2.f * qf - 1.f) / (1.f - 2.f * we);
-                } else {
-                    feq = (rho_o + 3.f * (1.f - 1.f / qf) * uc + 4.5f * uc * uc - 1.5f * usq) * ld.w;
-                    chi = we * (2.f * qf - 1.f);
-                }
-                v_link = (1.f - chi) * fb + chi * feq;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            v_out[k] = v_link[k] = v_fw[k] = 0.f;
+            if (has_out[k]) {
+                const float gq = 0.57735026919f - (out_axis[k] == 0 ? uo_[0] : out_axis[k] == 1 ? uo_[1] : uo_[2]);
+                v_out[k] = gq * f_in_cell[k] + (1.f - gq) * fo[k];
             }
-            v_fw = fb + v_link;
+            if (link[k]) {
+                if (a.wall == WALL_BB) {
+                    v_link[k] = fb[k];
+                } else {
+                    const float omega_l = a.omega[ic], rho_o = a.rho_p[ic], tau_o = a.tau_p[ic];
+                    const float usq = uo_[0] * uo_[0] + uo_[1] * uo_[1] + uo_[2] * uo_[2];
+                    const float sdf0 = a.sdf[ic];
+                    const float qf = fabsf(sdf0) / (fabsf(sdf0) + fabsf(sdf1[k]));
+                    const float we = 1.f / (1.f / omega_l + tau_o);
+                    const float uc =
+                        -uo_[0] * (float)ld[k].c[0] - uo_[1] * (float)ld[k].c[1] - uo_[2] * (float)ld[k].c[2];
+                    float feq, chi;
+                    if (qf <= 0.5f) {
+                        const float uf = -ufc[k][0] * (float)ld[k].c[0] - ufc[k][1] * (float)ld[k].c[1] -
+                                         ufc[k][2] * (float)ld[k].c[2];
+                        feq = (rho_o + 3.f * uf + 4.5f * uc * uc - 1.5f * usq) * ld[k].w;
+                        chi = we * (2.f * qf - 1.f) / (1.f - 2.f * we);
+                    } else {
+                        feq = (rho_o + 3.f * (1.f - 1.f / qf) * uc + 4.5f * uc * uc - 1.5f * usq) * ld[k].w;
+                        chi = we * (2.f * qf - 1.f);
+                    }
+                    v_link[k] = (1.f - chi) * fb[k] + chi * feq;
+                }
+                v_fw[k] = fb[k] + v_link[k];
+            }
         }
     } else if (a.border_pulls && (x[0] == 0 || x[0] == N[0] - 1 || x[1] == 0 || x[1] == N[1] - 1 || x[2] == 0 ||
                                   x[2] == N[2] - 1)) {
@@ -1451,12 +1475,12 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
             }
         }
         // outflowBC (Geier et al. 2015 App. F; kernel.cl:2005-2097)
-        if constexpr (WARP) {
+        if constexpr (GRP) {
             // the lanes' outlet values (computed from the same reads as below)
 #pragma unroll
             for (int q = 1; q < Q; q++) {
-                const float vq = __shfl_sync(0xffffffffu, v_out, q);
-                if (__shfl_sync(0xffffffffu, (int)has_out, q)) ft[q] = vq;
+                const float vq = __shfl_sync(gmask, v_out[q / G], q % G, G);
+                if (__shfl_sync(gmask, (int)has_out[q / G], q % G, G)) ft[q] = vq;
             }
         } else if (b[0] == BC_OUTLET || b[1] == BC_OUTLET || b[2] == BC_OUTLET) {
             const float cs = 0.57735026919f;
@@ -1481,14 +1505,17 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     // internalWallBC: STL links (kernel.cl:1926-2003 / D3Q27 1823-1897)
     float fw[3] = {0.f, 0.f, 0.f};
     const float omega = a.omega[ic];
-    if constexpr (WARP) {
+    if constexpr (GRP) {
         // the lanes' link results, and the momentum exchange summed in direction order
-        if (__any_sync(0xffffffffu, link)) {
+        bool any_link = false;
+#pragma unroll
+        for (int k = 0; k < K; k++) any_link |= link[k];
+        if (__any_sync(gmask, any_link)) {
 #pragma unroll
             for (int q = 1; q < Q; q++) {
-                const float vq = __shfl_sync(0xffffffffu, v_link, q);
-                const float sq = __shfl_sync(0xffffffffu, v_fw, q);
-                if (__shfl_sync(0xffffffffu, (int)link, q)) {
+                const float vq = __shfl_sync(gmask, v_link[q / G], q % G, G);
+                const float sq = __shfl_sync(gmask, v_fw[q / G], q % G, G);
+                if (__shfl_sync(gmask, (int)link[q / G], q % G, G)) {
                     ft[q] = vq;
 #pragma unroll
                     for (int d = 0; d < 3; d++)
@@ -1531,7 +1558,7 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
                 if (lat_c(Q, q, d)) fw[d] += -(fb + ft[q]) * (float)lat_c(Q, q, d);
         }
     }
-    if (!WARP || lane == 0) {
+    if (!GRP || lane == 0) {
         a.fwx[ic] = fw[0];
         a.fwy[ic] = fw[1];
         a.fwz[ic] = fw[2];
@@ -1557,7 +1584,7 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
         else tsgs = smagorinsky<Q>(ft, rho, u, v, w, omega, a.les, a.cs);
         tsgs = damping(a, tsgs, a.sdf[ic], u, v, w, omega);
     }
-    if (!WARP || lane == 0) {
+    if (!GRP || lane == 0) {
         a.rho_n[ic] = rho;
         a.u_n[ic] = u;
         a.v_n[ic] = v;
@@ -1572,12 +1599,16 @@ __device__ __forceinline__ void special_cell(const StepArgs& a, long long t)
     } else {
         collide<Q, COLL>(ft, rho, u, v, w, 1.f / (tau + tsgs), a);
     }
-    if constexpr (WARP) {
-        float mine = ft[0];
+    if constexpr (GRP) {
 #pragma unroll
-        for (int q = 1; q < Q; q++)
-            if (lane == q) mine = ft[q];
-        if (lane < Q) Codec<S>::store(static_cast<T*>(a.f_out) + (long long)lane * a.pE + ip, mine, ld.w);
+        for (int k = 0; k < K; k++) {
+            const int qk = lane + G * k;
+            float mine = ft[0];
+#pragma unroll
+            for (int q = 1; q < Q; q++)
+                if (qk == q) mine = ft[q];
+            if (qk < Q) Codec<S>::store(static_cast<T*>(a.f_out) + (long long)qk * a.pE + ip, mine, ld[k].w);
+        }
     } else {
 #pragma unroll
         for (int q = 0; q < Q; q++) Codec<S>::store(static_cast<T*>(a.fout_q[q]) + ip, ft[q], lat_w(Q, q));
@@ -1591,13 +1622,19 @@ __global__ void __launch_bounds__(SPECIAL_BS) k_special(const StepArgs a)
     if (t < a.n_special) special_cell<Q, S, COLL>(a, t);
 }
 
-// one warp per listed cell (special_cell with WARP): for short lists, where one thread per cell
-// leaves most SMs idle and each thread's chain of dependent reads sets the kernel's time
+// a group of LBFFS_SPECIAL_LANES lanes per listed cell (special_cell with G lanes): for short lists,
+// where one thread per cell leaves most SMs idle and each thread's chain of dependent reads sets the
+// kernel's time.  16 lanes (two cells per warp) measured 4 % faster on the 1024x256x4 channel than
+// 32 and 13 % faster than 8; a build-time tuning value
+#ifndef LBFFS_SPECIAL_LANES
+#define LBFFS_SPECIAL_LANES 16
+#endif
 template <int Q, int S, int COLL>
 __global__ void __launch_bounds__(SPECIAL_BS) k_special_warp(const StepArgs a)
 {
-    const long long t = (long long)blockIdx.x * (SPECIAL_BS / 32) + (threadIdx.x >> 5);
-    if (t < a.n_special) special_cell<Q, S, COLL, true>(a, t);
+    constexpr int G = LBFFS_SPECIAL_LANES;
+    const long long t = (long long)blockIdx.x * (SPECIAL_BS / G) + (threadIdx.x / G);
+    if (t < a.n_special) special_cell<Q, S, COLL, G>(a, t);
 }
 
 // ---- ghost layer: the reference's face streaming for populations that cross the grid edge ----

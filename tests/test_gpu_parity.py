@@ -152,8 +152,9 @@ def test_fp16s_boundary_cases_vs_fp64_oracle(cuda_lib, oracle_built, name):
                                   "density_q19_dpdx", "wallfn_q19", "step_q19_les", "step_q19_les_vandriest",
                                   "cavity_q19_wale", "ibm_q19"])
 def test_boundary_kernel_mappings_agree_bitwise(cuda_lib, name, storage):
-    """The boundary kernel with one thread per listed cell and with one warp per cell (lane q reading
-    direction q) computes the same bits: populations, macroscopic fields, eddy viscosity, wall force."""
+    """The boundary kernel with one thread per listed cell and with a lane group per cell (each lane
+    reading its directions) computes the same bits: populations, macroscopic fields, eddy viscosity,
+    wall force."""
     out = []
     for kind in (0, 1):
         _, _, lat = run_gpu(name, storage=storage, special_kernel=kind)
