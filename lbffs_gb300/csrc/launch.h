@@ -37,8 +37,9 @@ cudaError_t setup_scatter_special(const uint8_t* flags, long long E, uint8_t mas
 cudaError_t setup_link_masks(int Q, const uint32_t* special, long long n, const uint16_t* bc, const uint8_t* solid,
                              const uint8_t* nei, int nx, int ny, int nz, uint32_t* masks, cudaStream_t st);
 // rows [row0, row0 + nrows) of the packed population array (Q*ny*nz rows of nx floats) to / from
-// the padded device planes
-cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long row0, long long nrows,
+// the padded device planes (encode: into dst, and into dst2 when it is set); the packed array may be
+// pinned host memory the device addresses directly
+cudaError_t encode_f(int storage, int Q, const float* src, void* dst, void* dst2, long long row0, long long nrows,
                      const PadGeom& g, cudaStream_t st);
 cudaError_t decode_f(int storage, int Q, const void* src, float* dst, long long row0, long long nrows,
                      const PadGeom& g, cudaStream_t st);

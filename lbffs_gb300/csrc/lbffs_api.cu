@@ -486,6 +486,19 @@ static cudaError_t copy_planes_f32(lbffs_ctx* c, const float* host, bool upload)
     return e;
 }
 
+// The device address of page-locked host memory (cudaHostAlloc / cudaHostRegister), through which
+// the conversion kernels read or write the reference's packed population layout in one pass over
+// the host link; null for pageable memory, which goes through copies.
+static const void* pinned_device_ptr(const void* host)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t bytes)
 {
     if (!c || !host) return fail(c, LBFFS_E_ARG, "lbffs_upload: null argument");
@@ -505,6 +518,14 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
         const float* h = static_cast<const float*>(host);
         // both population copies get the uploaded values: initialization.hpp fills f and fTmp alike, and
         // cells that are never written (solid cells) must read the same values from either copy
+        if (const void* hd = pinned_device_ptr(host)) {
+            // pinned host memory: one kernel reads the packed rows over the host link and writes both
+            // padded copies (with the storage conversion)
+            CK(encode_f(c->d.storage, c->Q, static_cast<const float*>(hd), c->f[0], c->f[1], 0, rows, c->pg,
+                        c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            return LBFFS_OK;
+        }
         if (c->d.storage == LBFFS_FP32) {
             // FP32 is stored as is: one pitched copy per direction into the padded planes, then the
             // second copy device to device (no staging, no conversion kernel)
@@ -518,7 +539,7 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
             const long long n = (rows - r < chunk) ? rows - r : chunk;
             CK(cudaMemcpyAsync(c->stage, h + r * nx, (size_t)(n * nx) * sizeof(float), cudaMemcpyHostToDevice,
                                c->stream));
-            for (int b = 0; b < 2; b++) CK(encode_f(c->d.storage, c->Q, c->stage, c->f[b], r, n, c->pg, c->stream));
+            CK(encode_f(c->d.storage, c->Q, c->stage, c->f[0], c->f[1], r, n, c->pg, c->stream));
         }
         CK(cudaStreamSynchronize(c->stream));
         return LBFFS_OK;
@@ -552,6 +573,14 @@ extern "C" int lbffs_download(lbffs_ctx* c, int field, void* host, size_t bytes)
         const long long nx = c->d.nx;
         const long long rows = (long long)c->Q * c->d.ny * c->d.nz, chunk = (long long)c->stage_elems / nx;
         float* h = static_cast<float*>(host);
+        if (const void* hd = pinned_device_ptr(host)) {
+            // pinned host memory: one kernel reads the padded planes and writes the packed rows over
+            // the host link (with the storage conversion)
+            CK(decode_f(c->d.storage, c->Q, c->f[c->fcur], static_cast<float*>(const_cast<void*>(hd)), 0, rows,
+                        c->pg, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            return LBFFS_OK;
+        }
         if (c->d.storage == LBFFS_FP32) {
             CK(copy_planes_f32(c, h, false));
             CK(cudaStreamSynchronize(c->stream));

@@ -225,14 +225,20 @@ __device__ __forceinline__ long long padded_row(const PadGeom& g, long long r, i
     return (long long)q * g.pE + g.porg + (long long)k * g.pxy + (long long)j * g.px;
 }
 
+// src may be host memory the device can address (pinned); dst2, when set, receives the same values
 template <int S, int Q>
-__global__ void k_encode(const float* src, typename Codec<S>::T* dst, long long row0, PadGeom g)
+__global__ void k_encode(const float* src, typename Codec<S>::T* dst, typename Codec<S>::T* dst2, long long row0,
+                         PadGeom g)
 {
     int q;
     const long long base = padded_row(g, row0 + blockIdx.x, q);
     const float w = weight_of<Q>(q);
     const float* s = src + (long long)blockIdx.x * g.nx;
-    for (int i = threadIdx.x; i < g.nx; i += blockDim.x) Codec<S>::store(dst + base + i, s[i], w);
+    for (int i = threadIdx.x; i < g.nx; i += blockDim.x) {
+        const float v = s[i];
+        Codec<S>::store(dst + base + i, v, w);
+        if (dst2) Codec<S>::store(dst2 + base + i, v, w);
+    }
 }
 
 template <int S, int Q>
@@ -246,12 +252,14 @@ __global__ void k_decode(const typename Codec<S>::T* src, float* dst, long long 
 }
 
 template <int S>
-static cudaError_t enc_q(int Q, const float* src, void* dst, long long row0, long long nrows, const PadGeom& g,
-                         cudaStream_t st)
+static cudaError_t enc_q(int Q, const float* src, void* dst, void* dst2, long long row0, long long nrows,
+                         const PadGeom& g, cudaStream_t st)
 {
     using T = typename Codec<S>::T;
-    if (Q == 19) k_encode<S, 19><<<(unsigned)nrows, 256, 0, st>>>(src, static_cast<T*>(dst), row0, g);
-    else k_encode<S, 27><<<(unsigned)nrows, 256, 0, st>>>(src, static_cast<T*>(dst), row0, g);
+    if (Q == 19)
+        k_encode<S, 19><<<(unsigned)nrows, 256, 0, st>>>(src, static_cast<T*>(dst), static_cast<T*>(dst2), row0, g);
+    else
+        k_encode<S, 27><<<(unsigned)nrows, 256, 0, st>>>(src, static_cast<T*>(dst), static_cast<T*>(dst2), row0, g);
     return cudaGetLastError();
 }
 
@@ -265,14 +273,14 @@ static cudaError_t dec_q(int Q, const void* src, float* dst, long long row0, lon
     return cudaGetLastError();
 }
 
-cudaError_t encode_f(int storage, int Q, const float* src, void* dst, long long row0, long long nrows,
+cudaError_t encode_f(int storage, int Q, const float* src, void* dst, void* dst2, long long row0, long long nrows,
                      const PadGeom& g, cudaStream_t st)
 {
     if (nrows <= 0) return cudaSuccess;
     switch (storage) {
-        case ST_FP32: return enc_q<ST_FP32>(Q, src, dst, row0, nrows, g, st);
-        case ST_FP16S: return enc_q<ST_FP16S>(Q, src, dst, row0, nrows, g, st);
-        case ST_BF16S: return enc_q<ST_BF16S>(Q, src, dst, row0, nrows, g, st);
+        case ST_FP32: return enc_q<ST_FP32>(Q, src, dst, dst2, row0, nrows, g, st);
+        case ST_FP16S: return enc_q<ST_FP16S>(Q, src, dst, dst2, row0, nrows, g, st);
+        case ST_BF16S: return enc_q<ST_BF16S>(Q, src, dst, dst2, row0, nrows, g, st);
     }
     return cudaErrorInvalidValue;
 }
