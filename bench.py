@@ -318,6 +318,7 @@ def describe(name, storage):
 
 
 BULK_KIND = 0  # D3Q19 bulk kernel variant (--bulk-kind)
+BORDER_PULLS = 1  # face streaming read where it lies (1) or from a ghost layer filled every step (0)
 
 
 def run_device(name, storage, steps, warmup, device, timing_pass=True):
@@ -328,6 +329,7 @@ def run_device(name, storage, steps, warmup, device, timing_pass=True):
                     wall=sel["wall"], device=device, damping=sel.get("damping", "wall"))
     if c.q == 19:
         lat.set_bulk_kernel(BULK_KIND)
+    lat.set_border_pulls(BORDER_PULLS)
     if sel.get("rest"):
         for name in ("boundary", "boundary1", "boundary2", "boundary3", "u0", "v0", "w0", "solid", "nei_solid", "sdf",
                      "omega"):
@@ -540,12 +542,16 @@ def main():
                     help="serving workload: the served run alone, without the serial baselines")
     ap.add_argument("--bulk-kind", type=int, default=0, choices=[0, 1],
                     help="D3Q19 bulk kernel: 0 per-thread loads, 1 row-staged bulk copies")
+    ap.add_argument("--border-pulls", type=int, default=1, choices=[0, 1],
+                    help="1: populations crossing the grid's border read where the face streaming takes "
+                         "them (where the faces allow); 0: from a ghost layer filled before every step")
     ap.add_argument("--profile", action="store_true",
                     help="device-timed steps only (no e2e, CPU baseline or variants): the command ncu captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global BULK_KIND
+    global BULK_KIND, BORDER_PULLS
     BULK_KIND = args.bulk_kind
+    BORDER_PULLS = args.border_pulls
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -202,6 +202,14 @@ int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
 #define LBFFS_SPECIAL_WARP_MAX 16384
 int lbffs_set_special_kernel(lbffs_ctx* ctx, int kind);
 
+/* No counterpart in the reference (two ways to the same face streaming, which give identical
+   results).  enabled 1 (the default): where every face carries one boundary code per axis, the
+   step kernels read each population that crosses the grid's border where the face streaming takes
+   it (the periodic image, or the cell's own value of the bounce-back / mirror direction), and no
+   ghost layer is filled; 0: a ghost-layer fill before every step holds those values, and every
+   cell pulls from a fixed offset. */
+int lbffs_set_border_pulls(lbffs_ctx* ctx, int enabled);
+
 /* setSolid + setNeiSolid (src/walls.hpp:159-216) on the device, bit for bit the reference's host
    result: solid[ic] = 1 for cells inside the closed surface (ray-crossing parity of isInner,
    walls.hpp:73-157, within the STL's bounding box, which the reference starts at the origin),

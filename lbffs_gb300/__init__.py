@@ -108,6 +108,7 @@ def load_library():
         "lbffs_init_rest": ([vp], i),
         "lbffs_set_bulk_kernel": ([vp, i], i),
         "lbffs_set_special_kernel": ([vp, i], i),
+        "lbffs_set_border_pulls": ([vp, i], i),
         "lbffs_voxelize": ([vp, C.POINTER(C.c_float), C.c_longlong, i], i),
         "lbffs_output": ([vp, C.POINTER(OutputParams), C.POINTER(OutputResult)], i),
         "lbffs_write_vtk": ([vp, C.c_char_p, i, C.POINTER(OutputParams)], i),
@@ -258,6 +259,11 @@ class Lattice:
         """Boundary kernel mapping: 0 one thread per listed cell, 1 a lane group per cell, -1 by the
         list's length (same results)."""
         self._check(self.lib.lbffs_set_special_kernel(self.h, int(kind)))
+
+    def set_border_pulls(self, enabled):
+        """Face streaming across the grid's border: 1 (default) read where it takes each population
+        when the faces allow, 0 a ghost-layer fill before every step (same results)."""
+        self._check(self.lib.lbffs_set_border_pulls(self.h, int(enabled)))
 
     def init_rest(self):
         """Both population copies at rest (f_q = w_q) without a host upload."""

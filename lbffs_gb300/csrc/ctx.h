@@ -49,13 +49,16 @@ struct lbffs_ctx {
     int sponge_mask = 0;
     bool dirty = true;
     // pulls across the grid's border: face_ok when every face carries one boundary code per axis
-    // (face_codes, StepArgs layout) and the face flag is set on exactly the border cells; pull_ok
-    // when moreover both x faces carry boundary-kernel codes (inlet / outlet / fixed density / wall
-    // function), so bulk rows cross only y / z faces: the context (alone or served) then runs
-    // without a ghost layer
+    // (face_codes, StepArgs layout) and the face flag is set on exactly the border cells.  pull_mode
+    // (StepArgs::border_pulls) 1 when moreover both x faces carry boundary-kernel codes (inlet /
+    // outlet / fixed density / wall function), so bulk rows cross only y / z faces; 2 when bulk
+    // cells lie on the x faces (nz > 1); 0 otherwise.  A context with a pull mode (alone or served)
+    // runs without a ghost layer.
     int face_codes = 0;
     bool face_ok = false;
     bool pull_ok = false;
+    int pull_mode = 0;
+    bool pulls_on = true;  // lbffs_set_border_pulls
     int* d_err = nullptr;
     float* stage = nullptr;
     size_t stage_elems = 0;

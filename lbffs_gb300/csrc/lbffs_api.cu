@@ -393,13 +393,17 @@ static int commit(lbffs_ctx* c)
         ctx_free(c, bad);
         CK(e);
         c->face_ok = h == 0;
-        // the bulk kernels cross only y / z faces: both x faces must be boundary-kernel faces (x-face
-        // bulk cells reading across the x face measured slower than the ghost fill they save)
+        // mode 1: both x faces are boundary-kernel faces and the bulk kernels cross only y / z faces;
+        // mode 2: x-face bulk cells pull across the x face too, where that kernel is built (a 2D grid
+        // keeps the ghost layer: its x-face cells are face cells for the z-crossing directions where
+        // their row neighbours are not)
         auto kernel_face = [](int code) {
             return code == BC_OUTLET || code == BC_FIXVEL || code == BC_FIXDEN || code == BC_WALLFN;
         };
-        c->pull_ok = LBFFS_BORDER_PULLS && c->face_ok && kernel_face(c->face_codes & 7) &&
-                     kernel_face((c->face_codes >> 3) & 7);
+        const bool x_kernel = kernel_face(c->face_codes & 7) && kernel_face((c->face_codes >> 3) & 7);
+        const bool x_pulls = nz > 1 && xface_pulls_built(c->Q, c->d.storage == LBFFS_FP32 ? ST_FP32 : ST_FP16S);
+        c->pull_mode = !(LBFFS_BORDER_PULLS && c->face_ok) ? 0 : x_kernel ? 1 : x_pulls ? 2 : 0;
+        c->pull_ok = c->pull_mode != 0;
     }
     // uniform relaxation rate: the value at the domain centre
     const long long centre = ((long long)(nz / 2) * ny + ny / 2) * nx + nx / 2;
@@ -688,6 +692,29 @@ void lbffs::ctx_step_args(const lbffs_ctx* c, const lbffs_step_params* p, int sr
                                                    (uintptr_t)(pull * (long long)c->tsize));
         a.fout_q[q] = static_cast<char*>(a.f_out) + plane;
     }
+    // x-face pull bases (border_pulls 2): a cell on the low / high x face of a row that crosses no
+    // other face, its border codes (the x face's code, 0, 0) and face flag set (border_pull)
+    {
+        const int nx = c->d.nx;
+        const int code_lo = c->face_codes & 7;
+        const int code_hi = nx == 1 ? code_lo : (c->face_codes >> 3) & 7;
+        for (int q = 0; q < c->Q; q++) {
+            a.fin_xlo[q] = a.fin_s[q];
+            a.fin_xhi[q] = a.fin_s[q];
+            const int cx = lat_c(c->Q, q, 0);
+            if (cx == 0) continue;
+            const int code = cx > 0 ? code_lo : code_hi;
+            const void*& base = cx > 0 ? a.fin_xlo[q] : a.fin_xhi[q];
+            if (is_wall_code(code)) {
+                const int b[3] = {code, 0, 0};
+                base = a.fin_q[c->Q == 19 ? missing_dir<19>(q, b) : missing_dir<27>(q, b)];
+            } else {
+                // the periodic image: nx elements further (low face) or back (high face)
+                const long long sh = (cx > 0 ? nx : -nx) * (long long)c->tsize;
+                base = reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(a.fin_s[q]) + (uintptr_t)sh);
+            }
+        }
+    }
     float* const* mp = c->macro[msrc];
     float* const* mn = c->macro[1 - msrc];
     a.rho_p = mp[0];
@@ -742,12 +769,13 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
     // allow it (pull_ok: the x-face cells are boundary-kernel cells), nothing changes the produced
     // populations after the step (no IBM forcing pass) and the bulk kernel is the per-thread one;
     // otherwise from the ghost layer, filled before every step
-    const bool pulls = c->pull_ok && c->n_markers <= 1 && c->bulk_kind == 0;
+    const bool pulls = c->pull_ok && c->pulls_on && c->n_markers <= 1 && c->bulk_kind == 0;
+    const int pull_mode = pulls ? c->pull_mode : 0;
     for (int s = 0; s < nsteps; s++) {
         StepArgs a;
         ctx_step_args(c, p, c->fcur, c->mcur, a);
         a.store_all = (p->store_fields == 2) || (p->store_fields == 1 && s == nsteps - 1);
-        a.border_pulls = pulls ? 1 : 0;
+        a.border_pulls = pull_mode;
         // ghost layer of this step's source populations: the face streaming of the six faces
         if (!pulls) {
             cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1073,6 +1101,13 @@ extern "C" int lbffs_set_bulk_kernel(lbffs_ctx* c, int kind)
 {
     if (!c || kind < 0 || kind > 1) return fail(c, LBFFS_E_ARG, "lbffs_set_bulk_kernel: kind must be 0 or 1");
     c->bulk_kind = kind;
+    return LBFFS_OK;
+}
+
+extern "C" int lbffs_set_border_pulls(lbffs_ctx* c, int enabled)
+{
+    if (!c || enabled < 0 || enabled > 1) return fail(c, LBFFS_E_ARG, "lbffs_set_border_pulls: enabled must be 0 or 1");
+    c->pulls_on = enabled != 0;
     return LBFFS_OK;
 }
 

@@ -65,6 +65,11 @@ constexpr int BULK_V = 2;
 #ifndef LBFFS_BORDER_PULLS
 #define LBFFS_BORDER_PULLS 1
 #endif
+// the bulk kernels with pulls across the x faces (border_pulls 2) are built for D3Q19 and for FP32
+// D3Q27; with 2-byte D3Q27 storage they measured slower than the ghost fill they replace (the
+// 256^3 cavity: 0.430 against 0.419 ms per step), and those lattices keep the ghost layer
+__host__ __device__ constexpr bool xface_pulls_built(int Q, int S) { return Q == 19 || S == ST_FP32; }
+
 template <int Q, int COLL = 0, int SGS = 0>
 __host__ __device__ constexpr int bulk_v()
 {
@@ -111,6 +116,30 @@ __host__ __device__ constexpr int lat_find(int Q, int x, int y, int z)
 __host__ __device__ constexpr int lat_opp(int Q, int q)
 {
     return lat_find(Q, -lat_c(Q, q, 0), -lat_c(Q, q, 1), -lat_c(Q, q, 2));
+}
+
+// the wall codes: a population crossing a face with one of them is missing (bounce-back / mirror)
+__host__ __device__ __forceinline__ bool is_wall_code(int b) { return b == 1 || b == 4 || b == 5 || b == 6 || b == 7; }
+
+// bounce-back / mirror direction for a missing link on a domain face (reflectOrMirrorQ, D3Q19
+// kernel.cl:114-326; D3Q27 kernel.cl:1133-1146 with mirrorQx/y/z)
+template <int Q>
+__host__ __device__ __forceinline__ int missing_dir(int q, const int (&b)[3])
+{
+    const int c0 = lat_c(Q, q, 0), c1 = lat_c(Q, q, 1), c2 = lat_c(Q, q, 2);
+    const int r = lat_opp(Q, q);
+    if (Q == 19) {
+        if ((c0 != 0) + (c1 != 0) + (c2 != 0) < 2) return r;
+        if (c0 != 0 && b[0] == BC_SYM) return lat_find(Q, -c0, c1, c2);
+        if (c1 != 0 && b[1] == BC_SYM) return lat_find(Q, c0, -c1, c2);
+        if (c2 != 0 && b[2] == BC_SYM) return lat_find(Q, c0, c1, -c2);
+        return r;
+    }
+    int out = r;
+    if (b[0] == BC_SYM) out = c0 ? lat_find(Q, -c0, c1, c2) : r;
+    if (b[1] == BC_SYM) out = c1 ? lat_find(Q, c0, -c1, c2) : r;
+    if (b[2] == BC_SYM) out = c2 ? lat_find(Q, c0, c1, -c2) : r;
+    return out;
 }
 
 // ---- population storage codecs ----
@@ -208,10 +237,12 @@ struct StepArgs {
     int nx, ny, nz;
     float omega0, dpdx, les, omega_b, spz, clim, cs;
     int damping;      // near-wall damping of the Smagorinsky eddy viscosity (enum lbffs_damping)
-    // pulls across the grid's border: 0, from the ghost layer filled before each step (k_halo); 1,
-    // straight from where the face streaming takes them (every face carries one boundary code per
-    // axis: face_codes holds code (axis d, low / high face s) in bits 3 (2 d + s) .. 3 (2 d + s) + 2;
-    // both x faces carry boundary-kernel codes, so bulk cells cross only y / z faces)
+    // pulls across the grid's border: 0, from the ghost layer filled before each step (k_halo); 1 and
+    // 2, straight from where the face streaming takes them (every face carries one boundary code per
+    // axis: face_codes holds code (axis d, low / high face s) in bits 3 (2 d + s) .. 3 (2 d + s) + 2).
+    // 1: both x faces carry boundary-kernel codes, so bulk cells cross only y / z faces; 2: bulk
+    // cells lie on the x faces too (nz > 1), those of rows crossing no y / z face pulling their
+    // x-crossing directions from fin_xlo / fin_xhi
     int border_pulls;
     int face_codes;
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity
@@ -231,6 +262,12 @@ struct StepArgs {
     const void* fin_q[27];
     const void* fin_s[27];
     void* fout_q[27];
+    // border_pulls 2: the plane base from which a cell on the low (xlo, directions c_x > 0) / high
+    // (xhi, c_x < 0) x face of a row crossing no other face pulls: the base of the missing direction's
+    // own plane (fin_q) when the face carries a wall code, else the pull base shifted to the periodic
+    // image (fin_s -+ nx elements); the other directions' entries are fin_s
+    const void* fin_xlo[27];
+    const void* fin_xhi[27];
 };
 
 __host__ __device__ __forceinline__ int pidx(const StepArgs& a, int i, int j, int k)

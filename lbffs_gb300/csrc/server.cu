@@ -287,7 +287,9 @@ cudaError_t build_batch(lbffs_server* s)
                 // the resident cases together exceed L2, whatever one case's size: no policy
                 // (evict-first measured 3 % slower on the served sample)
                 hc[i].args[p].l2_policy = 0;
-                hc[i].args[p].border_pulls = c->pull_ok && c->n_markers <= 1 ? 1 : 0;
+                // the batched bulk kernels run no x-face pulls: a case with bulk cells on its x faces
+                // keeps the ghost layer
+                hc[i].args[p].border_pulls = c->pull_mode == 1 && c->pulls_on && c->n_markers <= 1 ? 1 : 0;
             }
             hc[i].last = hc[i].args[(r->nsteps - 1) & 1];
             hc[i].last.store_all = 1;

@@ -32,13 +32,20 @@ cudaError_t LBFFS_NAME(LBFFS_Q, LBFFS_S, LBFFS_C, LBFFS_PART)(const StepArgs& a,
 #else
     constexpr int V = bulk_v<LBFFS_Q, LBFFS_C, LBFFS_PART == 2 ? SGS_WALE : SGS_SMAG>();
     const dim3 grid((a.nx + BULK_BX * V - 1) / (BULK_BX * V), a.ny, a.nz);
-#if LBFFS_PART == 0
-    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_SMAG, false><<<grid, BULK_BX, 0, st>>>(a);
-#elif LBFFS_PART == 1
-    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_SMAG, true><<<grid, BULK_BX, 0, st>>>(a);
+    constexpr int SGS = LBFFS_PART == 2 ? SGS_WALE : SGS_SMAG;
+    constexpr bool LES = LBFFS_PART == 1;
+    // the x-face pull kernels where they are built (xface_pulls_built: D3Q19, FP32 D3Q27)
+#if LBFFS_Q == 19 || LBFFS_S == 0
+    static_assert(xface_pulls_built(LBFFS_Q, LBFFS_S), "x-face pull kernel list");
+    if (a.border_pulls == 2) {
+        k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS, LES, true><<<grid, BULK_BX, 0, st>>>(a);
+        return cudaGetLastError();
+    }
 #else
-    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS_WALE, false><<<grid, BULK_BX, 0, st>>>(a);
+    static_assert(!xface_pulls_built(LBFFS_Q, LBFFS_S), "x-face pull kernel list");
+    if (a.border_pulls == 2) return cudaErrorInvalidValue;  // the context never selects a mode without its kernel
 #endif
+    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS, LES, false><<<grid, BULK_BX, 0, st>>>(a);
 #endif
     return cudaGetLastError();
 }

@@ -241,7 +241,6 @@ __device__ __forceinline__ float calc_tauw(float rhow, float magUp, float nu)
 }
 
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ bool is_wall_code(int b) { return b == 1 || b == 4 || b == 5 || b == 6 || b == 7; }
 
 // upwindID_B with per-axis wall codes (face cells) or plain periodic wrap (other cells); -1 = missing
 template <int Q>
@@ -260,27 +259,6 @@ __device__ __forceinline__ long long upwind(int q, const int (&x)[3], const int 
         }
     }
     return ((long long)n[2] * N[1] + n[1]) * N[0] + n[0];
-}
-
-// bounce-back / mirror direction for a missing link on a domain face (reflectOrMirrorQ, D3Q19
-// kernel.cl:114-326; D3Q27 kernel.cl:1133-1146 with mirrorQx/y/z)
-template <int Q>
-__device__ __forceinline__ int missing_dir(int q, const int (&b)[3])
-{
-    const int c0 = lat_c(Q, q, 0), c1 = lat_c(Q, q, 1), c2 = lat_c(Q, q, 2);
-    const int r = lat_opp(Q, q);
-    if (Q == 19) {
-        if ((c0 != 0) + (c1 != 0) + (c2 != 0) < 2) return r;
-        if (c0 != 0 && b[0] == BC_SYM) return lat_find(Q, -c0, c1, c2);
-        if (c1 != 0 && b[1] == BC_SYM) return lat_find(Q, c0, -c1, c2);
-        if (c2 != 0 && b[2] == BC_SYM) return lat_find(Q, c0, c1, -c2);
-        return r;
-    }
-    int out = r;
-    if (b[0] == BC_SYM) out = c0 ? lat_find(Q, -c0, c1, c2) : r;
-    if (b[1] == BC_SYM) out = c1 ? lat_find(Q, c0, -c1, c2) : r;
-    if (b[2] == BC_SYM) out = c2 ? lat_find(Q, c0, c1, -c2) : r;
-    return out;
 }
 
 // ---- border pulls (StepArgs::border_pulls 1): the face streaming without a ghost layer ----
@@ -324,12 +302,36 @@ __device__ __forceinline__ BorderCell border_cell(const StepArgs& a, int i, int 
     return g;
 }
 
-// The border of a bulk row (j, k) in a border-pull context: bulk cells are never x-face cells there,
-// so only the y / z faces are crossed (row_crosses: the row lies on one of them).  The row's x flags
-// and x code are left clear, so every bulk cell of the row shares the mapping.
+// The border of a bulk row (j, k) in a border-pull context: the y / z faces it crosses (row_crosses:
+// the row lies on one of them).  row_border leaves the row's x flags and x code clear, so every
+// cell of the row off the x faces shares its mapping; the cells of such a row take border_cell.
 __device__ __forceinline__ bool row_crosses(const StepArgs& a, int j, int k)
 {
     return a.border_pulls && (j == 0 || j == a.ny - 1 || k == 0 || k == a.nz - 1);
+}
+
+// border_pulls 2 (bulk cells on the x faces; the bulk kernels' XF instantiations): cell i of a row
+// lies on an x face.  In a row that crosses no y / z face such a cell pulls its x-crossing directions
+// (c_x > 0 on the low face, c_x < 0 on the high face) from the plane bases fin_xlo / fin_xhi and every
+// other direction as any cell; in a row that crosses one it takes its own border (border_cell) for
+// the directions with c_x != 0.
+__device__ __forceinline__ bool xface_cell(const StepArgs& a, int i) { return i == 0 || i == a.nx - 1; }
+
+// the x-face bits of a pair of cells i0 < i1 of rows crossing no y / z face (-1: no cell): bit 0, i0
+// on the low face; bit 1, i0 on the high face; bit 2, i1 on the high face
+__device__ __forceinline__ int xface_bits(const StepArgs& a, int i0, int i1)
+{
+    return (i0 == 0 ? 1 : 0) | (i0 == a.nx - 1 ? 2 : 0) | (i1 == a.nx - 1 ? 4 : 0);
+}
+
+// the plane base direction q of a cell at the low (lo) / high (hi) x face of a row crossing no other
+// face pulls from
+template <int Q>
+__device__ __forceinline__ const void* xface_base(const StepArgs& a, int q, bool lo, bool hi)
+{
+    if (lat_c(Q, q, 0) > 0 && lo) return a.fin_xlo[q];
+    if (lat_c(Q, q, 0) < 0 && hi) return a.fin_xhi[q];
+    return a.fin_s[q];
 }
 __device__ __forceinline__ BorderCell row_border(const StepArgs& a, int j, int k)
 {
@@ -601,15 +603,17 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[Q], co
 }
 
 // Two cells of one thread through bulk_collide2, then the stores of the active ones.
-template <int S, bool LES>
+template <int S, bool LES, bool XF = false>
 __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                           const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
                                           const int (&ic)[2], const int (&ip)[2], bool plain = false)
 {
     using T = typename Codec<S>::T;
     F2 ft[19];
-    if (row_crosses(a, cj[0], ck[0]) || row_crosses(a, cj[1], ck[1])) {
-        const BorderCell rb[2] = {row_border(a, cj[0], ck[0]), row_border(a, cj[1], ck[1])};
+    if (row_crosses(a, cj[0], ck[0]) || row_crosses(a, cj[1], ck[1]) ||
+        (XF && (xface_cell(a, ci[0]) || xface_cell(a, ci[1])))) {
+        const BorderCell rb[2] = {XF ? border_cell(a, ci[0], cj[0], ck[0]) : row_border(a, cj[0], ck[0]),
+                                  XF ? border_cell(a, ci[1], cj[1], ck[1]) : row_border(a, cj[1], ck[1])};
         const T* f = static_cast<const T*>(a.f_in);
 #pragma unroll
         for (int q = 0; q < 19; q++) {
@@ -698,16 +702,22 @@ __device__ __forceinline__ float held_bits(__nv_bfloat16, uint16_t b) { return _
 // the Q pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol; BORDER:
 // the row crosses a y / z face (rb: its border, border pulls; both cells share its mapping, so the
 // pulls with c_x = 0 stay one aligned 32-bit word)
-template <int S, bool HINT, int Q = 19, bool BORDER = false>
+// BORDER 1: the pair's row crosses a y / z face and neither cell is a bulk cell on an x face: both take
+// the row's border rb[0].  BORDER 2: rb[0] the row's border, by which the c_x = 0 pulls of every cell
+// of the row go (one word for the pair), rb[1 + v] the border of cell v, by which its other pulls go.
+// XF: a cell of the pair is on an x face of a row crossing no other face (xf bit 0: cell 0 on the
+// low face, bit 1: cell 0 on the high face, bit 2: cell 1 on the high face).
+template <int S, bool HINT, int Q = 19, int BORDER = 0, bool XF = false>
 __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool any, [[maybe_unused]] uint64_t pol,
-                                              F2 (&ft)[Q], [[maybe_unused]] const BorderCell* rb = nullptr)
+                                              F2 (&ft)[Q], [[maybe_unused]] const BorderCell* rb = nullptr,
+                                              [[maybe_unused]] int xf = 0)
 {
     using T = typename Codec<S>::T;
     static_assert(sizeof(T) == 2, "2-byte storage");
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         const T* p;
-        if constexpr (BORDER) p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, *rb, q, ip0);
+        if constexpr (BORDER != 0) p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb[0], q, ip0);
         else p = static_cast<const T*>(a.fin_s[q]) + ip0;
         if (lat_c(Q, q, 0) == 0) {
             uint32_t wd = 0u;
@@ -715,13 +725,22 @@ __device__ __forceinline__ void pair_adj_load(const StepArgs& a, int ip0, bool a
             else wd = any ? __ldg(reinterpret_cast<const unsigned int*>(p)) : 0u;
             ft[q] = held_unpack(T{}, wd);
         } else {
+            const T* p1 = p + 1;
+            if constexpr (BORDER == 2) {
+                p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb[1], q, ip0);
+                p1 = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb[2], q, ip0 + 1);
+            }
+            if constexpr (XF) {
+                p = static_cast<const T*>(xface_base<Q>(a, q, xf & 1, xf & 2)) + ip0;
+                p1 = static_cast<const T*>(xface_base<Q>(a, q, false, xf & 4)) + ip0 + 1;
+            }
             float x0, x1;
             if constexpr (HINT) {
                 x0 = any ? held_bits(T{}, ld_hint_b16(p, pol)) : 0.f;
-                x1 = any ? held_bits(T{}, ld_hint_b16(p + 1, pol)) : 0.f;
+                x1 = any ? held_bits(T{}, ld_hint_b16(p1, pol)) : 0.f;
             } else {
                 x0 = any ? Codec<S>::load_held(p) : 0.f;
-                x1 = any ? Codec<S>::load_held(p + 1) : 0.f;
+                x1 = any ? Codec<S>::load_held(p1) : 0.f;
             }
             ft[q] = pk(x0, x1);
         }
@@ -757,15 +776,26 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
 // pulls with c_x = 0 of both cells are one aligned 32-bit word (the pull offset c_y px + c_z pxy is
 // even), and when both cells are active their results leave as one packed 32-bit store.  Both
 // cells' pulls are read when either is active (the row is padded by a ghost cell on each side).
-template <int S, bool LES>
+template <int S, bool LES, bool XF = false>
 __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                               const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
                                               const int (&ic)[2], int ip0, bool plain = false)
 {
     F2 ft[19];
+    const int xf = XF ? xface_bits(a, ci[0], ci[1]) : 0;
     if (row_crosses(a, cj[0], ck[0])) {
-        const BorderCell rb = row_border(a, cj[0], ck[0]);
-        pair_adj_load<S, false, 19, true>(a, ip0, act[0] || act[1], 0, ft, &rb);
+        if constexpr (XF) {
+            const BorderCell rb[3] = {row_border(a, cj[0], ck[0]), border_cell(a, ci[0], cj[0], ck[0]),
+                                      border_cell(a, ci[1], cj[1], ck[1])};
+            pair_adj_load<S, false, 19, 2>(a, ip0, act[0] || act[1], 0, ft, rb);
+        } else {
+            const BorderCell rb = row_border(a, cj[0], ck[0]);
+            pair_adj_load<S, false, 19, 1>(a, ip0, act[0] || act[1], 0, ft, &rb);
+        }
+        bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
+        pair_adj_store<S, false>(a, ft, act, ip0, 0);
+    } else if (xf != 0) {
+        if constexpr (XF) pair_adj_load<S, false, 19, 0, true>(a, ip0, act[0] || act[1], 0, ft, nullptr, xf);
         bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
         pair_adj_store<S, false>(a, ft, act, ip0, 0);
     } else if (LBFFS_BULK_EVICT && a.l2_policy != 0) {
@@ -811,7 +841,7 @@ __device__ __forceinline__ void bulk_prefetch(const StepArgs& a)
 // The adjacent pair of a bulk_block lane with its pulls issued together with its flag loads
 // (one memory round trip before the collision instead of two): the pair's pulls are read whenever
 // its first cell is in the row, active or not (a solid cell's values are read and dropped).
-template <int S, bool LES, int Q = 19>
+template <int S, bool LES, int Q = 19, bool XF = false>
 __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, int j, int k, int row, int prow,
                                                     bool inrange = true)
 {
@@ -822,9 +852,22 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
     const bool hint = LBFFS_BULK_EVICT && a.l2_policy != 0;
     [[maybe_unused]] uint64_t pol = 0;
     F2 ft[Q];
+    int xf = 0;
+    bool xany = false;
+    if constexpr (XF) {
+        xf = valid ? xface_bits(a, i0, i0 + 1) : 0;
+        xany = __any_sync(0xffffffffu, xf != 0);
+    }
     if (row_crosses(a, j, k)) {
-        const BorderCell rb = row_border(a, j, k);
-        pair_adj_load<S, false, Q, true>(a, prow + i0, valid, 0, ft, &rb);
+        if constexpr (XF) {
+            const BorderCell rb[3] = {row_border(a, j, k), border_cell(a, i0, j, k), border_cell(a, i0 + 1, j, k)};
+            pair_adj_load<S, false, Q, 2>(a, prow + i0, valid, 0, ft, rb);
+        } else {
+            const BorderCell rb = row_border(a, j, k);
+            pair_adj_load<S, false, Q, 1>(a, prow + i0, valid, 0, ft, &rb);
+        }
+    } else if (xany) {
+        if constexpr (XF) pair_adj_load<S, false, Q, 0, true>(a, prow + i0, valid, 0, ft, nullptr, xf);
     } else if (hint) {
         pol = a.l2_policy == 1 ? l2_policy_evict_first() : l2_policy_evict_normal();
         pair_adj_load<S, true, Q>(a, prow + i0, valid, pol, ft);
@@ -844,7 +887,7 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
 
 // bulk_pair (cells i0 and i0 + 32) with the pulls issued together with the flag loads; a cell's
 // pulls are read whenever it is in the row, active or not
-template <int S, bool LES, int Q = 19>
+template <int S, bool LES, int Q = 19, bool XF = false>
 __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j, int k, int row, int prow)
 {
     using T = typename Codec<S>::T;
@@ -853,13 +896,34 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
     F2 ft[Q];
 #pragma unroll
     for (int v = 0; v < 2; v++) fl[v] = valid[v] ? __ldg(a.flags + row + i0 + 32 * v) : FL_SOLID;
+    int xf = 0;
+    bool xany = false;
+    if constexpr (XF) {
+        xf = xface_bits(a, valid[0] ? i0 : -1, valid[1] ? i0 + 32 : -1);
+        xany = __any_sync(0xffffffffu, xf != 0);
+    }
     if (row_crosses(a, j, k)) {
-        const BorderCell rb = row_border(a, j, k);
+        // the c_x = 0 pulls by the row's border (one mapping for the row), the others by the cell's own
+        // (XF) or the row's
+        const BorderCell rb[3] = {row_border(a, j, k), XF ? border_cell(a, i0, j, k) : row_border(a, j, k),
+                                  XF ? border_cell(a, i0 + 32, j, k) : row_border(a, j, k)};
+        const T* f = static_cast<const T*>(a.f_in);
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            const T* p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb, q, prow + i0);
+            const bool cx0 = !XF || lat_c(Q, q, 0) == 0;
+            const T* p = f + border_pull<Q>(a, cx0 ? rb[0] : rb[1], q, prow + i0);
+            const T* p1 = cx0 ? p + 32 : f + border_pull<Q>(a, rb[2], q, prow + i0 + 32);
             const float x0 = valid[0] ? Codec<S>::load_held(p) : 0.f;
-            const float x1 = valid[1] ? Codec<S>::load_held(p + 32) : 0.f;
+            const float x1 = valid[1] ? Codec<S>::load_held(p1) : 0.f;
+            ft[q] = pk(x0, x1);
+        }
+    } else if (XF && xany) {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const T* p = static_cast<const T*>(xface_base<Q>(a, q, xf & 1, xf & 2)) + prow + i0;
+            const T* p1 = static_cast<const T*>(xface_base<Q>(a, q, false, xf & 4)) + prow + i0 + 32;
+            const float x0 = valid[0] ? Codec<S>::load_held(p) : 0.f;
+            const float x1 = valid[1] ? Codec<S>::load_held(p1) : 0.f;
             ft[q] = pk(x0, x1);
         }
     } else {
@@ -892,7 +956,7 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
 // with the reference's face streaming at the start of the step.
 // One CTA tile: BULK_BX * bulk_v<Q>() cells of row (j, k) starting at x-block xb.  PF: the tile is
 // CTA (xb, j, k) of a k_bulk grid, so the L2 prefetch of the tiles launched later may run.
-template <int Q, int S, int COLL, int SGS, bool LES, bool PF = true>
+template <int Q, int S, int COLL, int SGS, bool LES, bool PF = true, bool XF = false>
 __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int k)
 {
     using T = typename Codec<S>::T;
@@ -912,15 +976,15 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     const int prow = pidx(a, 0, j, k);
     if constexpr (PF) bulk_prefetch<Q, S, V>(a);
     if constexpr (PAIR27) {
-        if constexpr (S != ST_FP32) bulk_pair_adj_eager<S, LES, 27>(a, base + 2 * lane, j, k, row, prow);
-        else bulk_pair_eager<S, LES, 27>(a, base + lane, j, k, row, prow);
+        if constexpr (S != ST_FP32) bulk_pair_adj_eager<S, LES, 27, XF>(a, base + 2 * lane, j, k, row, prow);
+        else bulk_pair_eager<S, LES, 27, XF>(a, base + lane, j, k, row, prow);
         return;
     }
     if constexpr (ADJ && LBFFS_BULK_EAGER) {
-        bulk_pair_adj_eager<S, LES>(a, i0, j, k, row, prow);
+        bulk_pair_adj_eager<S, LES, 19, XF>(a, i0, j, k, row, prow);
         return;
     } else if constexpr (Q == 19 && SGS != SGS_WALE && V == 2 && !ADJ && LBFFS_BULK_EAGER32) {
-        bulk_pair_eager<S, LES>(a, i0, j, k, row, prow);
+        bulk_pair_eager<S, LES, 19, XF>(a, i0, j, k, row, prow);
         return;
     }
     uint8_t fl[V];
@@ -939,11 +1003,11 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     if constexpr (ADJ) {
         const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 1};
-        bulk_pair_adj<S, LES>(a, fl, act, ci, cj, ck, ic, prow + i0, plain);
+        bulk_pair_adj<S, LES, XF>(a, fl, act, ci, cj, ck, ic, prow + i0, plain);
     } else if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) {
         const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
-        bulk_pair<S, LES>(a, fl, act, ci, cj, ck, ic, ip, plain);
+        bulk_pair<S, LES, XF>(a, fl, act, ci, cj, ck, ic, ip, plain);
     } else {
         float ft[V][Q];
         const bool cross = row_crosses(a, j, k);
@@ -951,8 +1015,8 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         for (int v = 0; v < V; v++) {
             if (!act[v]) continue;
             const int ip = prow + i0 + DV * v;
-            if (cross) {
-                const BorderCell rb = row_border(a, j, k);
+            if (cross || (XF && xface_cell(a, i0 + DV * v))) {
+                const BorderCell rb = XF ? border_cell(a, i0 + DV * v, j, k) : row_border(a, j, k);
 #pragma unroll
                 for (int q = 0; q < Q; q++) {
                     const T* p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb, q, ip);
@@ -1118,10 +1182,11 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
 #define LBFFS_BULK_BOUNDS(Q, LES) \
     __launch_bounds__(BULK_BX, (Q) == 19 ? LBFFS_BULK_MINB19 : (LES) ? LBFFS_BULK_MINB27_LES : LBFFS_BULK_MINB27)
 
-template <int Q, int S, int COLL, int SGS, bool LES>
+// XF: the lattice's bulk cells lie on the x faces and pull across them (border_pulls 2)
+template <int Q, int S, int COLL, int SGS, bool LES, bool XF>
 __global__ void LBFFS_BULK_BOUNDS(Q, LES) k_bulk(const StepArgs a)
 {
-    bulk_block<Q, S, COLL, SGS, LES>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+    bulk_block<Q, S, COLL, SGS, LES, true, XF>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ---- a lane group per boundary cell (special_cell with G lanes) ----

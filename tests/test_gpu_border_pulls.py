@@ -68,3 +68,58 @@ def test_border_pulls_match_oracle(cuda_lib, oracle_built, storage, q, kind, nx,
         tol = 1e-5 * np.abs(g).max() if storage == "fp32" else 2e-5
         bad = np.argwhere(d > tol)
         assert len(bad) == 0, (steps, float(d.max()), sorted(set(bad[:, 3].tolist()))[:8])
+
+
+def _mode_case(q, kind, nx, nz):
+    if kind == "cavity":
+        faces = K.cavity_faces(0.05)
+    elif kind == "channel":
+        faces = K.channel_faces(0.05)
+    else:
+        faces = _faces(kind.replace("_solid", ""), nz)
+    solid = None
+    if kind.endswith("_solid"):
+        # solid blocks on both x faces: link cells of the boundary kernel beside bulk cells there
+        s = np.zeros((nz, 12, nx), np.uint8)
+        s[1:3, 3:6, 0:3] = 1
+        s[2:4, 6:9, nx - 2:] = 1
+        solid = s.ravel()
+    c = K.make_case(nx, 12, nz, q, faces, nu=0.02, solid=solid)
+    rng = np.random.default_rng(nx + 7 * nz + q)
+    c.f = (c.f + 2e-3 * rng.standard_normal(c.f.shape)).astype(np.float32)
+    return c
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "bf16s"])
+@pytest.mark.parametrize("q,collision,sgs,les", [(19, "rr", "smag", 0.0), (19, "rr", "smag", 0.12),
+                                                 (19, "rr", "wale", 0.0), (27, "rr", "smag", 0.12),
+                                                 (27, "cumulant", "smag", 0.0)])
+@pytest.mark.parametrize("kind,nx,nz", [("cavity", 37, 6), ("cavity", 301, 3), ("walls_x", 64, 4),
+                                        ("symmetry_x", 33, 3), ("periodic_x", 70, 5), ("walls_x_solid", 45, 5),
+                                        ("channel", 40, 4), ("walls_x", 40, 1)])
+def test_pull_modes_agree_bitwise(cuda_lib, storage, q, collision, sgs, les, kind, nx, nz):
+    """Reading every population that crosses the grid's border where the face streaming takes it gives
+    the bits of reading it from a ghost layer filled before every step: populations and macroscopic
+    fields after 5 steps.  Bulk cells lie on the x faces here (cavity, walls, symmetry, periodic x;
+    odd row lengths and a second row tile end on an x face in either cell of a pair), beside
+    boundary-kernel cells (the solid blocks' links, the lid), or only boundary-kernel cells do (the
+    channel's inlet and outlet).  A 2D grid, and D3Q27 with 2-byte storage where bulk cells lie on the
+    x faces, keep the ghost layer in both settings."""
+    import lbffs_gb300 as L
+    c = _mode_case(q, kind, nx, nz)
+    out, halos = [], []
+    for on in (1, 0):
+        lat = L.Lattice(c.nx, c.ny, c.nz, q=q, storage=storage, collision=collision, sgs=sgs)
+        lat.set_border_pulls(on)
+        lat.set_timing(True)
+        lat.load_case(c)
+        lat.step(5, les=les)
+        lat.synchronize()
+        halos.append(lat.kernel_time("halo")[1])
+        out.append([lat.download(k) for k in ("f", "rho", "u", "v", "w")])
+        lat.close()
+    assert halos[1] == 5
+    ghost = kind != "channel" and (nz == 1 or (q == 27 and storage != "fp32"))
+    assert halos[0] == (5 if ghost else 0)
+    for k, (x, y) in enumerate(zip(*out)):
+        assert np.array_equal(x, y), (k, float(np.abs(x - y).max()))
