@@ -51,13 +51,17 @@ struct lbffs_ctx {
     // pulls across the grid's border: face_ok when every face carries one boundary code per axis
     // (face_codes, StepArgs layout) and the face flag is set on exactly the border cells.  pull_mode
     // (StepArgs::border_pulls) 1 when moreover both x faces carry boundary-kernel codes (inlet /
-    // outlet / fixed density / wall function), so bulk rows cross only y / z faces; 2 when bulk
-    // cells lie on the x faces (nz > 1); 0 otherwise.  A context with a pull mode (alone or served)
-    // runs without a ghost layer.
+    // outlet / fixed density / wall function), so bulk rows cross only y / z faces; with bulk cells on
+    // the x faces (nz > 1) 3 when neither x face is Cyclic (those cells write the x ghost slots they
+    // pull from next step themselves), else 2 (they pull across the x face from per-context plane
+    // bases) where that kernel is built; 0 otherwise.  Modes 1 and 2 run without a ghost fill; mode
+    // 3 fills the ghost layer once, before its first step from a state the pushes did not write
+    // (xghost_ok false).
     int face_codes = 0;
     bool face_ok = false;
     bool pull_ok = false;
     int pull_mode = 0;
+    bool xghost_ok = false;
     bool pulls_on = true;  // lbffs_set_border_pulls
     int* d_err = nullptr;
     float* stage = nullptr;

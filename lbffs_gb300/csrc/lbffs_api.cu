@@ -346,6 +346,7 @@ static int build_list(lbffs_ctx* c, uint8_t mask, uint32_t** list, long long* n)
 static int commit(lbffs_ctx* c)
 {
     const int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
+    c->xghost_ok = false;
     const long long E = c->E;
     // validate boundary codes on the device
     {
@@ -394,15 +395,22 @@ static int commit(lbffs_ctx* c)
         CK(e);
         c->face_ok = h == 0;
         // mode 1: both x faces are boundary-kernel faces and the bulk kernels cross only y / z faces;
-        // mode 2: x-face bulk cells pull across the x face too, where that kernel is built (a 2D grid
-        // keeps the ghost layer: its x-face cells are face cells for the z-crossing directions where
-        // their row neighbours are not)
+        // modes 3 and 2: x-face bulk cells take their x-crossing pulls through ghost slots they write
+        // themselves (no Cyclic x face: the value is the cell's own) or from per-context plane bases
+        // (where that kernel is built).  A 2D grid keeps the ghost layer: its x-face cells are face
+        // cells for the z-crossing directions where their row neighbours are not.
         auto kernel_face = [](int code) {
             return code == BC_OUTLET || code == BC_FIXVEL || code == BC_FIXDEN || code == BC_WALLFN;
         };
         const bool x_kernel = kernel_face(c->face_codes & 7) && kernel_face((c->face_codes >> 3) & 7);
-        const bool x_pulls = nz > 1 && xface_pulls_built(c->Q, c->d.storage == LBFFS_FP32 ? ST_FP32 : ST_FP16S);
-        c->pull_mode = !(LBFFS_BORDER_PULLS && c->face_ok) ? 0 : x_kernel ? 1 : x_pulls ? 2 : 0;
+        const bool x_cyclic = (c->face_codes & 7) == BC_CYCLIC || ((c->face_codes >> 3) & 7) == BC_CYCLIC;
+        const bool x_pulls = xface_pulls_built(c->Q, c->d.storage == LBFFS_FP32 ? ST_FP32 : ST_FP16S);
+        c->pull_mode = !(LBFFS_BORDER_PULLS && c->face_ok) ? 0
+                       : x_kernel                            ? 1
+                       : nz <= 1                             ? 0
+                       : !x_cyclic                           ? 3
+                       : x_pulls                             ? 2
+                                                             : 0;
         c->pull_ok = c->pull_mode != 0;
     }
     // uniform relaxation rate: the value at the domain centre
@@ -517,6 +525,7 @@ extern "C" int lbffs_upload(lbffs_ctx* c, int field, const void* host, size_t by
     CK(cudaSetDevice(c->d.device));
     FieldInfo fi = field_info(field);
     if (fi.kind == K_F) {
+        c->xghost_ok = false;
         const long long nx = c->d.nx;
         const long long rows = (long long)c->Q * c->d.ny * c->d.nz, chunk = (long long)c->stage_elems / nx;
         const float* h = static_cast<const float*>(host);
@@ -776,8 +785,9 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
         ctx_step_args(c, p, c->fcur, c->mcur, a);
         a.store_all = (p->store_fields == 2) || (p->store_fields == 1 && s == nsteps - 1);
         a.border_pulls = pull_mode;
-        // ghost layer of this step's source populations: the face streaming of the six faces
-        if (!pulls) {
+        // ghost layer of this step's source populations: the face streaming of the six faces (mode 3:
+        // once, when the x-face cells did not write their slots in the step that made the source)
+        if (pull_mode == 0 || (pull_mode == 3 && !c->xghost_ok)) {
             cudaEvent_t e0 = nullptr, e1 = nullptr;
             if (c->timing) {
                 e0 = get_event(c);
@@ -863,6 +873,7 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
         }
         c->fcur = 1 - c->fcur;
         c->mcur = 1 - c->mcur;
+        c->xghost_ok = pull_mode == 3;
     }
     return LBFFS_OK;
 }
@@ -1082,6 +1093,7 @@ extern "C" int lbffs_init_rest(lbffs_ctx* c)
 {
     if (!c) return fail(c, LBFFS_E_ARG, "lbffs_init_rest: null context");
     CK(cudaSetDevice(c->d.device));
+    c->xghost_ok = false;
     const size_t plane_bytes = (size_t)c->pg.pE * c->tsize;
     for (int b = 0; b < 2; b++) {
         if (c->d.storage == LBFFS_FP32) {
@@ -1108,6 +1120,7 @@ extern "C" int lbffs_set_border_pulls(lbffs_ctx* c, int enabled)
 {
     if (!c || enabled < 0 || enabled > 1) return fail(c, LBFFS_E_ARG, "lbffs_set_border_pulls: enabled must be 0 or 1");
     c->pulls_on = enabled != 0;
+    c->xghost_ok = false;
     return LBFFS_OK;
 }
 

@@ -240,9 +240,10 @@ struct StepArgs {
     // pulls across the grid's border: 0, from the ghost layer filled before each step (k_halo); 1 and
     // 2, straight from where the face streaming takes them (every face carries one boundary code per
     // axis: face_codes holds code (axis d, low / high face s) in bits 3 (2 d + s) .. 3 (2 d + s) + 2).
-    // 1: both x faces carry boundary-kernel codes, so bulk cells cross only y / z faces; 2: bulk
+    // 1: both x faces carry boundary-kernel codes, so bulk cells cross only y / z faces; 2 and 3: bulk
     // cells lie on the x faces too (nz > 1), those of rows crossing no y / z face pulling their
-    // x-crossing directions from fin_xlo / fin_xhi
+    // x-crossing directions from fin_xlo / fin_xhi (2) or from the ghost slots at x = -1 / nx, which
+    // they write for the next step after their collision (3: no Cyclic x face)
     int border_pulls;
     int face_codes;
     int sponge_mask;  // bit s set: face centre s (x-,x+,y-,y+,z-,z+) is Outlet/FixedDensity

@@ -177,6 +177,7 @@ bool admit_one(lbffs_server* s, Request* r)
         return false;
     }
     c->fcur = c->mcur = 0;
+    c->xghost_ok = false;
     r->ctx = c;
     {
         std::lock_guard<std::mutex> lock(s->mu);
@@ -414,6 +415,7 @@ void retire(lbffs_server* s, Request* r)
     c->stage = s->stage2;
     const long long parity = r->nsteps & 1;
     c->fcur = c->mcur = (int)parity;
+    c->xghost_ok = false;
     const size_t E = (size_t)c->E;
     int err_word = 0;
     cudaMemcpyAsync(&err_word, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);

@@ -34,18 +34,22 @@ cudaError_t LBFFS_NAME(LBFFS_Q, LBFFS_S, LBFFS_C, LBFFS_PART)(const StepArgs& a,
     const dim3 grid((a.nx + BULK_BX * V - 1) / (BULK_BX * V), a.ny, a.nz);
     constexpr int SGS = LBFFS_PART == 2 ? SGS_WALE : SGS_SMAG;
     constexpr bool LES = LBFFS_PART == 1;
+    if (a.border_pulls == 3) {  // x-face cells write their ghost slots
+        k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS, LES, 2><<<grid, BULK_BX, 0, st>>>(a);
+        return cudaGetLastError();
+    }
     // the x-face pull kernels where they are built (xface_pulls_built: D3Q19, FP32 D3Q27)
 #if LBFFS_Q == 19 || LBFFS_S == 0
     static_assert(xface_pulls_built(LBFFS_Q, LBFFS_S), "x-face pull kernel list");
     if (a.border_pulls == 2) {
-        k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS, LES, true><<<grid, BULK_BX, 0, st>>>(a);
+        k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS, LES, 1><<<grid, BULK_BX, 0, st>>>(a);
         return cudaGetLastError();
     }
 #else
     static_assert(!xface_pulls_built(LBFFS_Q, LBFFS_S), "x-face pull kernel list");
     if (a.border_pulls == 2) return cudaErrorInvalidValue;  // the context never selects a mode without its kernel
 #endif
-    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS, LES, false><<<grid, BULK_BX, 0, st>>>(a);
+    k_bulk<LBFFS_Q, LBFFS_S, LBFFS_C, SGS, LES, 0><<<grid, BULK_BX, 0, st>>>(a);
 #endif
     return cudaGetLastError();
 }

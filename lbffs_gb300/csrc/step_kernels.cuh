@@ -310,11 +310,13 @@ __device__ __forceinline__ bool row_crosses(const StepArgs& a, int j, int k)
     return a.border_pulls && (j == 0 || j == a.ny - 1 || k == 0 || k == a.nz - 1);
 }
 
-// border_pulls 2 (bulk cells on the x faces; the bulk kernels' XF instantiations): cell i of a row
-// lies on an x face.  In a row that crosses no y / z face such a cell pulls its x-crossing directions
-// (c_x > 0 on the low face, c_x < 0 on the high face) from the plane bases fin_xlo / fin_xhi and every
-// other direction as any cell; in a row that crosses one it takes its own border (border_cell) for
-// the directions with c_x != 0.
+// Bulk cells on the x faces (border_pulls 2 and 3; the bulk kernels' XM 1 and 2 instantiations):
+// xface_cell, cell i of a row lies on an x face.  In a row that crosses a y / z face such a cell takes
+// its own border (border_cell) for the directions with c_x != 0.  In a row that crosses no other face
+// it pulls its x-crossing directions (c_x > 0 on the low face, c_x < 0 on the high face) from the
+// plane bases fin_xlo / fin_xhi (XM 1, any x-face codes), or from the ghost slots at x = -1 / nx
+// like every other cell, which it wrote itself at the end of the previous step (XM 2, x faces
+// without a Cyclic code: xface_push).
 __device__ __forceinline__ bool xface_cell(const StepArgs& a, int i) { return i == 0 || i == a.nx - 1; }
 
 // the x-face bits of a pair of cells i0 < i1 of rows crossing no y / z face (-1: no cell): bit 0, i0
@@ -333,6 +335,7 @@ __device__ __forceinline__ const void* xface_base(const StepArgs& a, int q, bool
     if (lat_c(Q, q, 0) < 0 && hi) return a.fin_xhi[q];
     return a.fin_s[q];
 }
+
 __device__ __forceinline__ BorderCell row_border(const StepArgs& a, int j, int k)
 {
     BorderCell g;
@@ -603,7 +606,7 @@ __device__ __forceinline__ void bulk_collide2(const StepArgs& a, F2 (&ft)[Q], co
 }
 
 // Two cells of one thread through bulk_collide2, then the stores of the active ones.
-template <int S, bool LES, bool XF = false>
+template <int S, bool LES, int XM = 0>
 __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                           const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
                                           const int (&ic)[2], const int (&ip)[2], bool plain = false)
@@ -611,9 +614,9 @@ __device__ __forceinline__ void bulk_pair(const StepArgs& a, const uint8_t (&fl)
     using T = typename Codec<S>::T;
     F2 ft[19];
     if (row_crosses(a, cj[0], ck[0]) || row_crosses(a, cj[1], ck[1]) ||
-        (XF && (xface_cell(a, ci[0]) || xface_cell(a, ci[1])))) {
-        const BorderCell rb[2] = {XF ? border_cell(a, ci[0], cj[0], ck[0]) : row_border(a, cj[0], ck[0]),
-                                  XF ? border_cell(a, ci[1], cj[1], ck[1]) : row_border(a, cj[1], ck[1])};
+        (XM != 0 && (xface_cell(a, ci[0]) || xface_cell(a, ci[1])))) {
+        const BorderCell rb[2] = {XM ? border_cell(a, ci[0], cj[0], ck[0]) : row_border(a, cj[0], ck[0]),
+                                  XM ? border_cell(a, ci[1], cj[1], ck[1]) : row_border(a, cj[1], ck[1])};
         const T* f = static_cast<const T*>(a.f_in);
 #pragma unroll
         for (int q = 0; q < 19; q++) {
@@ -699,6 +702,45 @@ __device__ __forceinline__ void st_hint_b32(void* p, uint32_t v, uint64_t pol)
 __device__ __forceinline__ float held_bits(__half, uint16_t b) { return __half2float(__ushort_as_half(b)); }
 __device__ __forceinline__ float held_bits(__nv_bfloat16, uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
 
+// XM 2: an active bulk cell on the low (hi false) / high x face of a row crossing no y / z face, lane
+// L of the pair ft, at padded index ip, after its collision: for each direction q crossing its face
+// inward (c_x > 0 on the low face, c_x < 0 on the high one), the value its next step pulls from the
+// ghost position ip - c_q of plane q, which the face streaming takes from the cell itself — its new
+// value of the missing direction (missing_dir with the face's code: the x mirror on a Symmetry face,
+// else the opposite direction), stored as the row stores it.  The slot at x = -1, and at x = nx when
+// the row fills whole 32-byte sectors, is alone in its sector, which is written whole (the value
+// replicated) so that L2 need not merge a partial sector.
+template <int Q, int S, int L>
+__device__ __forceinline__ void xface_push(const StepArgs& a, const F2 (&ft)[Q], bool hi, int ip)
+{
+    using T = typename Codec<S>::T;
+    constexpr int A = 32 / (int)sizeof(T);
+    const int code = hi ? (a.face_codes >> 3) & 7 : a.face_codes & 7;
+    const bool sym = code == BC_SYM;
+    const bool whole = !hi || a.nx % A == 0;
+#pragma unroll
+    for (int q = 1; q < Q; q++) {
+        const int cx = lat_c(Q, q, 0), cy = lat_c(Q, q, 1), cz = lat_c(Q, q, 2);
+        if (cx == 0) continue;
+        if ((cx < 0) != hi) continue;
+        const int r = lat_opp(Q, q), m = lat_find(Q, -cx, cy, cz);
+        const F2 src = sym ? ft[m] : ft[r];
+        const float v = L == 0 ? lane0(src) : lane1(src);
+        T* p = static_cast<T*>(a.fout_q[q]) + (ip - (cx + cy * a.px + cz * a.pxy));
+        if (whole) {
+            uint32_t w32;
+            if constexpr (sizeof(T) == 4) w32 = __float_as_uint(v);
+            else w32 = held_pack(T{}, v, v);
+            const uint4 quad = make_uint4(w32, w32, w32, w32);
+            uint4* sec = reinterpret_cast<uint4*>(hi ? p : p - (A - 1));
+            sec[0] = quad;
+            sec[1] = quad;
+        } else {
+            Codec<S>::store_held(p, v);
+        }
+    }
+}
+
 // the Q pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol; BORDER:
 // the row crosses a y / z face (rb: its border, border pulls; both cells share its mapping, so the
 // pulls with c_x = 0 stay one aligned 32-bit word)
@@ -776,15 +818,15 @@ __device__ __forceinline__ void pair_adj_store(const StepArgs& a, const F2 (&ft)
 // pulls with c_x = 0 of both cells are one aligned 32-bit word (the pull offset c_y px + c_z pxy is
 // even), and when both cells are active their results leave as one packed 32-bit store.  Both
 // cells' pulls are read when either is active (the row is padded by a ghost cell on each side).
-template <int S, bool LES, bool XF = false>
+template <int S, bool LES, int XM = 0>
 __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (&fl)[2], const bool (&act)[2],
                                               const int (&ci)[2], const int (&cj)[2], const int (&ck)[2],
                                               const int (&ic)[2], int ip0, bool plain = false)
 {
     F2 ft[19];
-    const int xf = XF ? xface_bits(a, ci[0], ci[1]) : 0;
-    if (row_crosses(a, cj[0], ck[0])) {
-        if constexpr (XF) {
+    const bool xcell = XM != 0 && (xface_cell(a, ci[0]) || xface_cell(a, ci[1]));
+    if (row_crosses(a, cj[0], ck[0]) || xcell) {
+        if constexpr (XM != 0) {
             const BorderCell rb[3] = {row_border(a, cj[0], ck[0]), border_cell(a, ci[0], cj[0], ck[0]),
                                       border_cell(a, ci[1], cj[1], ck[1])};
             pair_adj_load<S, false, 19, 2>(a, ip0, act[0] || act[1], 0, ft, rb);
@@ -792,10 +834,6 @@ __device__ __forceinline__ void bulk_pair_adj(const StepArgs& a, const uint8_t (
             const BorderCell rb = row_border(a, cj[0], ck[0]);
             pair_adj_load<S, false, 19, 1>(a, ip0, act[0] || act[1], 0, ft, &rb);
         }
-        bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
-        pair_adj_store<S, false>(a, ft, act, ip0, 0);
-    } else if (xf != 0) {
-        if constexpr (XF) pair_adj_load<S, false, 19, 0, true>(a, ip0, act[0] || act[1], 0, ft, nullptr, xf);
         bulk_collide2<S, LES>(a, ft, fl, act, ci, cj, ck, ic, plain);
         pair_adj_store<S, false>(a, ft, act, ip0, 0);
     } else if (LBFFS_BULK_EVICT && a.l2_policy != 0) {
@@ -841,7 +879,7 @@ __device__ __forceinline__ void bulk_prefetch(const StepArgs& a)
 // The adjacent pair of a bulk_block lane with its pulls issued together with its flag loads
 // (one memory round trip before the collision instead of two): the pair's pulls are read whenever
 // its first cell is in the row, active or not (a solid cell's values are read and dropped).
-template <int S, bool LES, int Q = 19, bool XF = false>
+template <int S, bool LES, int Q = 19, int XM = 0>
 __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, int j, int k, int row, int prow,
                                                     bool inrange = true)
 {
@@ -852,14 +890,13 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
     const bool hint = LBFFS_BULK_EVICT && a.l2_policy != 0;
     [[maybe_unused]] uint64_t pol = 0;
     F2 ft[Q];
-    int xf = 0;
+    const bool cross = row_crosses(a, j, k);
+    // the pair's x-face cells in a row crossing no y / z face
+    const int xf = XM != 0 && valid && !cross ? xface_bits(a, i0, i0 + 1) : 0;
     bool xany = false;
-    if constexpr (XF) {
-        xf = valid ? xface_bits(a, i0, i0 + 1) : 0;
-        xany = __any_sync(0xffffffffu, xf != 0);
-    }
-    if (row_crosses(a, j, k)) {
-        if constexpr (XF) {
+    if constexpr (XM == 1) xany = __any_sync(0xffffffffu, xf != 0);
+    if (cross) {
+        if constexpr (XM != 0) {
             const BorderCell rb[3] = {row_border(a, j, k), border_cell(a, i0, j, k), border_cell(a, i0 + 1, j, k)};
             pair_adj_load<S, false, Q, 2>(a, prow + i0, valid, 0, ft, rb);
         } else {
@@ -867,7 +904,7 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
             pair_adj_load<S, false, Q, 1>(a, prow + i0, valid, 0, ft, &rb);
         }
     } else if (xany) {
-        if constexpr (XF) pair_adj_load<S, false, Q, 0, true>(a, prow + i0, valid, 0, ft, nullptr, xf);
+        if constexpr (XM == 1) pair_adj_load<S, false, Q, 0, true>(a, prow + i0, valid, 0, ft, nullptr, xf);
     } else if (hint) {
         pol = a.l2_policy == 1 ? l2_policy_evict_first() : l2_policy_evict_normal();
         pair_adj_load<S, true, Q>(a, prow + i0, valid, pol, ft);
@@ -881,13 +918,21 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
     if (!(act[0] || act[1])) return;
     const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
     bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain, &side);
+    // the ghost slots first: the populations are all live until the row stores anyway
+    if constexpr (XM == 2) {
+        if (xf != 0) {  // one or two lanes of the row's first and last warp
+            if ((xf & 1) && act[0]) xface_push<Q, S, 0>(a, ft, false, prow + i0);
+            if ((xf & 2) && act[0]) xface_push<Q, S, 0>(a, ft, true, prow + i0);
+            if ((xf & 4) && act[1]) xface_push<Q, S, 1>(a, ft, true, prow + i0 + 1);
+        }
+    }
     if (hint) pair_adj_store<S, true, Q>(a, ft, act, prow + i0, pol);
     else pair_adj_store<S, false, Q>(a, ft, act, prow + i0, 0);
 }
 
 // bulk_pair (cells i0 and i0 + 32) with the pulls issued together with the flag loads; a cell's
 // pulls are read whenever it is in the row, active or not
-template <int S, bool LES, int Q = 19, bool XF = false>
+template <int S, bool LES, int Q = 19, int XM = 0>
 __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j, int k, int row, int prow)
 {
     using T = typename Codec<S>::T;
@@ -896,28 +941,27 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
     F2 ft[Q];
 #pragma unroll
     for (int v = 0; v < 2; v++) fl[v] = valid[v] ? __ldg(a.flags + row + i0 + 32 * v) : FL_SOLID;
-    int xf = 0;
+    const bool cross = row_crosses(a, j, k);
+    // the pair's x-face cells in a row crossing no y / z face
+    const int xf = XM != 0 && !cross ? xface_bits(a, valid[0] ? i0 : -1, valid[1] ? i0 + 32 : -1) : 0;
     bool xany = false;
-    if constexpr (XF) {
-        xf = xface_bits(a, valid[0] ? i0 : -1, valid[1] ? i0 + 32 : -1);
-        xany = __any_sync(0xffffffffu, xf != 0);
-    }
-    if (row_crosses(a, j, k)) {
+    if constexpr (XM == 1) xany = __any_sync(0xffffffffu, xf != 0);
+    if (cross) {
         // the c_x = 0 pulls by the row's border (one mapping for the row), the others by the cell's own
-        // (XF) or the row's
-        const BorderCell rb[3] = {row_border(a, j, k), XF ? border_cell(a, i0, j, k) : row_border(a, j, k),
-                                  XF ? border_cell(a, i0 + 32, j, k) : row_border(a, j, k)};
+        // (x-face kernels) or the row's
+        const BorderCell rb[3] = {row_border(a, j, k), XM ? border_cell(a, i0, j, k) : row_border(a, j, k),
+                                  XM ? border_cell(a, i0 + 32, j, k) : row_border(a, j, k)};
         const T* f = static_cast<const T*>(a.f_in);
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            const bool cx0 = !XF || lat_c(Q, q, 0) == 0;
+            const bool cx0 = XM == 0 || lat_c(Q, q, 0) == 0;
             const T* p = f + border_pull<Q>(a, cx0 ? rb[0] : rb[1], q, prow + i0);
             const T* p1 = cx0 ? p + 32 : f + border_pull<Q>(a, rb[2], q, prow + i0 + 32);
             const float x0 = valid[0] ? Codec<S>::load_held(p) : 0.f;
             const float x1 = valid[1] ? Codec<S>::load_held(p1) : 0.f;
             ft[q] = pk(x0, x1);
         }
-    } else if (XF && xany) {
+    } else if (XM == 1 && xany) {
 #pragma unroll
         for (int q = 0; q < Q; q++) {
             const T* p = static_cast<const T*>(xface_base<Q>(a, q, xf & 1, xf & 2)) + prow + i0;
@@ -942,6 +986,14 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
     if (!(act[0] || act[1])) return;
     const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
     bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain, &side);
+    // the ghost slots first: the populations are all live until the row stores anyway
+    if constexpr (XM == 2) {
+        if (xf != 0) {  // one lane of the row's first and of its last warp
+            if ((xf & 1) && act[0]) xface_push<Q, S, 0>(a, ft, false, prow + i0);
+            if ((xf & 2) && act[0]) xface_push<Q, S, 0>(a, ft, true, prow + i0);
+            if ((xf & 4) && act[1]) xface_push<Q, S, 1>(a, ft, true, prow + i0 + 32);
+        }
+    }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         T* p = static_cast<T*>(a.fout_q[q]) + prow + i0;
@@ -956,7 +1008,7 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
 // with the reference's face streaming at the start of the step.
 // One CTA tile: BULK_BX * bulk_v<Q>() cells of row (j, k) starting at x-block xb.  PF: the tile is
 // CTA (xb, j, k) of a k_bulk grid, so the L2 prefetch of the tiles launched later may run.
-template <int Q, int S, int COLL, int SGS, bool LES, bool PF = true, bool XF = false>
+template <int Q, int S, int COLL, int SGS, bool LES, bool PF = true, int XM = 0>
 __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int k)
 {
     using T = typename Codec<S>::T;
@@ -976,15 +1028,15 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     const int prow = pidx(a, 0, j, k);
     if constexpr (PF) bulk_prefetch<Q, S, V>(a);
     if constexpr (PAIR27) {
-        if constexpr (S != ST_FP32) bulk_pair_adj_eager<S, LES, 27, XF>(a, base + 2 * lane, j, k, row, prow);
-        else bulk_pair_eager<S, LES, 27, XF>(a, base + lane, j, k, row, prow);
+        if constexpr (S != ST_FP32) bulk_pair_adj_eager<S, LES, 27, XM>(a, base + 2 * lane, j, k, row, prow);
+        else bulk_pair_eager<S, LES, 27, XM>(a, base + lane, j, k, row, prow);
         return;
     }
     if constexpr (ADJ && LBFFS_BULK_EAGER) {
-        bulk_pair_adj_eager<S, LES, 19, XF>(a, i0, j, k, row, prow);
+        bulk_pair_adj_eager<S, LES, 19, XM>(a, i0, j, k, row, prow);
         return;
     } else if constexpr (Q == 19 && SGS != SGS_WALE && V == 2 && !ADJ && LBFFS_BULK_EAGER32) {
-        bulk_pair_eager<S, LES, 19, XF>(a, i0, j, k, row, prow);
+        bulk_pair_eager<S, LES, 19, XM>(a, i0, j, k, row, prow);
         return;
     }
     uint8_t fl[V];
@@ -1003,11 +1055,11 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
     if constexpr (ADJ) {
         const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 1};
-        bulk_pair_adj<S, LES, XF>(a, fl, act, ci, cj, ck, ic, prow + i0, plain);
+        bulk_pair_adj<S, LES, XM>(a, fl, act, ci, cj, ck, ic, prow + i0, plain);
     } else if constexpr (Q == 19 && SGS != SGS_WALE && V == 2) {
         const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
         const int ic[2] = {row + i0, row + i0 + 32}, ip[2] = {prow + i0, prow + i0 + 32};
-        bulk_pair<S, LES, XF>(a, fl, act, ci, cj, ck, ic, ip, plain);
+        bulk_pair<S, LES, XM>(a, fl, act, ci, cj, ck, ic, ip, plain);
     } else {
         float ft[V][Q];
         const bool cross = row_crosses(a, j, k);
@@ -1015,8 +1067,8 @@ __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int
         for (int v = 0; v < V; v++) {
             if (!act[v]) continue;
             const int ip = prow + i0 + DV * v;
-            if (cross || (XF && xface_cell(a, i0 + DV * v))) {
-                const BorderCell rb = XF ? border_cell(a, i0 + DV * v, j, k) : row_border(a, j, k);
+            if (cross || (XM != 0 && xface_cell(a, i0 + DV * v))) {
+                const BorderCell rb = XM ? border_cell(a, i0 + DV * v, j, k) : row_border(a, j, k);
 #pragma unroll
                 for (int q = 0; q < Q; q++) {
                     const T* p = static_cast<const T*>(a.f_in) + border_pull<Q>(a, rb, q, ip);
@@ -1182,11 +1234,13 @@ __device__ __forceinline__ void bulk_segments(const StepArgs& a, int g0, int spr
 #define LBFFS_BULK_BOUNDS(Q, LES) \
     __launch_bounds__(BULK_BX, (Q) == 19 ? LBFFS_BULK_MINB19 : (LES) ? LBFFS_BULK_MINB27_LES : LBFFS_BULK_MINB27)
 
-// XF: the lattice's bulk cells lie on the x faces and pull across them (border_pulls 2)
-template <int Q, int S, int COLL, int SGS, bool LES, bool XF>
+// XM: bulk cells on the x faces pull across them from per-context plane bases (1, border_pulls 2)
+// or through ghost slots they write themselves (2, border_pulls 3); 0: no bulk cell on an x face
+// pulls across it from where it lies (border_pulls 0 and 1)
+template <int Q, int S, int COLL, int SGS, bool LES, int XM>
 __global__ void LBFFS_BULK_BOUNDS(Q, LES) k_bulk(const StepArgs a)
 {
-    bulk_block<Q, S, COLL, SGS, LES, true, XF>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+    bulk_block<Q, S, COLL, SGS, LES, true, XM>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ---- a lane group per boundary cell (special_cell with G lanes) ----

@@ -97,14 +97,34 @@ def _mode_case(q, kind, nx, nz):
 @pytest.mark.parametrize("kind,nx,nz", [("cavity", 37, 6), ("cavity", 301, 3), ("walls_x", 64, 4),
                                         ("symmetry_x", 33, 3), ("periodic_x", 70, 5), ("walls_x_solid", 45, 5),
                                         ("channel", 40, 4), ("walls_x", 40, 1)])
+def _expected_halos(kind, q, storage, nz, steps):
+    """Ghost fills a run of `steps` steps launches: none where the lattice pulls across all its faces
+    (inlet / outlet x faces; Cyclic x faces where that kernel is built), one where the x-face cells
+    write their own ghost slots (x faces without a Cyclic code: the fill before the first step), one
+    per step otherwise (a 2D grid; D3Q27 2-byte storage with Cyclic x faces)."""
+    if kind == "channel":
+        return 0
+    if nz == 1:
+        return steps
+    if kind == "periodic_x":
+        return 0 if (q == 19 or storage == "fp32") else steps
+    return 1
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16s", "bf16s"])
+@pytest.mark.parametrize("q,collision,sgs,les", [(19, "rr", "smag", 0.0), (19, "rr", "smag", 0.12),
+                                                 (19, "rr", "wale", 0.0), (27, "rr", "smag", 0.12),
+                                                 (27, "rr", "smag", 0.0), (27, "cumulant", "smag", 0.0)])
+@pytest.mark.parametrize("kind,nx,nz", [("cavity", 37, 6), ("cavity", 301, 3), ("walls_x", 64, 4),
+                                        ("symmetry_x", 33, 3), ("periodic_x", 70, 5), ("walls_x_solid", 45, 5),
+                                        ("channel", 40, 4), ("walls_x", 40, 1)])
 def test_pull_modes_agree_bitwise(cuda_lib, storage, q, collision, sgs, les, kind, nx, nz):
     """Reading every population that crosses the grid's border where the face streaming takes it gives
     the bits of reading it from a ghost layer filled before every step: populations and macroscopic
     fields after 5 steps.  Bulk cells lie on the x faces here (cavity, walls, symmetry, periodic x;
     odd row lengths and a second row tile end on an x face in either cell of a pair), beside
     boundary-kernel cells (the solid blocks' links, the lid), or only boundary-kernel cells do (the
-    channel's inlet and outlet).  A 2D grid, and D3Q27 with 2-byte storage where bulk cells lie on the
-    x faces, keep the ghost layer in both settings."""
+    channel's inlet and outlet).  A 2D grid keeps the ghost layer in both settings."""
     import lbffs_gb300 as L
     c = _mode_case(q, kind, nx, nz)
     out, halos = [], []
@@ -119,7 +139,38 @@ def test_pull_modes_agree_bitwise(cuda_lib, storage, q, collision, sgs, les, kin
         out.append([lat.download(k) for k in ("f", "rho", "u", "v", "w")])
         lat.close()
     assert halos[1] == 5
-    ghost = kind != "channel" and (nz == 1 or (q == 27 and storage != "fp32"))
-    assert halos[0] == (5 if ghost else 0)
+    assert halos[0] == _expected_halos(kind, q, storage, nz, 5)
+    for k, (x, y) in enumerate(zip(*out)):
+        assert np.array_equal(x, y), (k, float(np.abs(x - y).max()))
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16s"])
+@pytest.mark.parametrize("q", [19, 27])
+def test_ghost_slots_follow_state_changes(cuda_lib, storage, q):
+    """Where x-face cells write their own ghost slots, every change of the populations from outside a
+    step (an upload, a rest state, a switch of the pull setting) makes the next step fill the ghost
+    layer first: a run interrupted by each of them gives the bits of the ghost-layer run."""
+    import lbffs_gb300 as L
+    c = _mode_case(q, "cavity", 45, 5)
+    rng = np.random.default_rng(5)
+    f2 = (c.f + 1e-3 * rng.standard_normal(c.f.shape)).astype(np.float32)
+    out, halos = [], []
+    for on in (1, 0):
+        lat = L.Lattice(c.nx, c.ny, c.nz, q=q, storage=storage)
+        lat.set_border_pulls(on)
+        lat.set_timing(True)
+        lat.load_case(c)
+        lat.step(3)
+        lat.upload("f", f2)
+        lat.step(2)
+        lat.set_border_pulls(on)
+        lat.step(2)
+        lat.init_rest()
+        lat.step(2)
+        lat.synchronize()
+        halos.append(lat.kernel_time("halo")[1])
+        out.append([lat.download(k) for k in ("f", "rho", "u", "v", "w")])
+        lat.close()
+    assert halos == [4, 9]
     for k, (x, y) in enumerate(zip(*out)):
         assert np.array_equal(x, y), (k, float(np.abs(x - y).max()))
