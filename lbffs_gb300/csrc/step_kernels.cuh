@@ -702,14 +702,9 @@ __device__ __forceinline__ void st_hint_b32(void* p, uint32_t v, uint64_t pol)
 __device__ __forceinline__ float held_bits(__half, uint16_t b) { return __half2float(__ushort_as_half(b)); }
 __device__ __forceinline__ float held_bits(__nv_bfloat16, uint16_t b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
 
-// XM 2: an active bulk cell on the low (hi false) / high x face of a row crossing no y / z face, lane
-// L of the pair ft, at padded index ip, after its collision: for each direction q crossing its face
-// inward (c_x > 0 on the low face, c_x < 0 on the high one), the value its next step pulls from the
-// ghost position ip - c_q of plane q, which the face streaming takes from the cell itself — its new
-// value of the missing direction (missing_dir with the face's code: the x mirror on a Symmetry face,
-// else the opposite direction), stored as the row stores it.  The slot at x = -1, and at x = nx when
-// the row fills whole 32-byte sectors, is alone in its sector, which is written whole (the value
-// replicated) so that L2 need not merge a partial sector.
+// XM 2: the ghost slots of an active bulk cell on the low (hi false) / high x face of a row crossing
+// no y / z face, lane L of the pair ft, at padded index ip, after its collision, written by its own
+// thread (the D3Q19 kernels; see xface_push_warp for what is written where).
 template <int Q, int S, int L>
 __device__ __forceinline__ void xface_push(const StepArgs& a, const F2 (&ft)[Q], bool hi, int ip)
 {
@@ -721,8 +716,7 @@ __device__ __forceinline__ void xface_push(const StepArgs& a, const F2 (&ft)[Q],
 #pragma unroll
     for (int q = 1; q < Q; q++) {
         const int cx = lat_c(Q, q, 0), cy = lat_c(Q, q, 1), cz = lat_c(Q, q, 2);
-        if (cx == 0) continue;
-        if ((cx < 0) != hi) continue;
+        if (cx == 0 || (cx < 0) != hi) continue;
         const int r = lat_opp(Q, q), m = lat_find(Q, -cx, cy, cz);
         const F2 src = sym ? ft[m] : ft[r];
         const float v = L == 0 ? lane0(src) : lane1(src);
@@ -739,6 +733,79 @@ __device__ __forceinline__ void xface_push(const StepArgs& a, const F2 (&ft)[Q],
             Codec<S>::store_held(p, v);
         }
     }
+}
+
+// XM 2, a pair's x-face cells (xf: xface_bits, act: its active cells), by the lane's own thread
+template <int Q, int S>
+__device__ __forceinline__ void xface_push_lane(const StepArgs& a, const F2 (&ft)[Q], int xf, const bool (&act)[2],
+                                                int ip0, int ip1)
+{
+    if ((xf & 1) && act[0]) xface_push<Q, S, 0>(a, ft, false, ip0);
+    if ((xf & 2) && act[0]) xface_push<Q, S, 0>(a, ft, true, ip0);
+    if ((xf & 4) && act[1]) xface_push<Q, S, 1>(a, ft, true, ip1);
+}
+
+// XM 2: the ghost slots of a warp's x-face cell, written by the warp's lanes together (every lane
+// of the warp calls, with the same arguments).  The cell is on the low (HI false) / high x face of a
+// row crossing no y / z face, cell `second` of lane src's pair ft, at padded index ip, after its
+// collision.  For each direction q crossing its face inward (c_x > 0 on the low face, c_x < 0 on the
+// high one; 5 for D3Q19, 9 for D3Q27) its next step pulls from the ghost position ip - c_q of plane
+// q a value the face streaming takes from the cell itself: its new value of the missing direction
+// (missing_dir with the face's code: the x mirror on a Symmetry face, else the opposite
+// direction), stored as the row stores it.  The values reach the lanes by shuffles, lane 2 n + h
+// writing half h of direction n's slot: the slot at x = -1, and at x = nx when the row fills whole
+// 32-byte sectors, is alone in its sector, which is written whole (the value replicated) so that
+// L2 need not merge a partial sector; otherwise lane 2 n writes the element.  The D3Q27 kernels
+// write their 9 slots per face this way; the D3Q19 ones, whose 5 slots one thread writes in turn
+// (xface_push), measured faster with the serial form (the cavity's FP16S step 0.264 against 0.269 ms;
+// D3Q27 FP16S 0.390 against 0.403 ms the other way round).
+template <int Q, int S, bool HI>
+__device__ __forceinline__ void xface_push_warp(const StepArgs& a, const F2 (&ft)[Q], int src, bool second, int ip)
+{
+    using T = typename Codec<S>::T;
+    constexpr int A = 32 / (int)sizeof(T);
+    const int lane = threadIdx.x & 31, slot = lane >> 1, half = lane & 1;
+    const int code = HI ? (a.face_codes >> 3) & 7 : a.face_codes & 7;
+    const bool sym = code == BC_SYM;
+    float mine = 0.f;
+    T* p = nullptr;
+    int n = 0;
+#pragma unroll
+    for (int q = 1; q < Q; q++) {
+        const int cx = lat_c(Q, q, 0), cy = lat_c(Q, q, 1), cz = lat_c(Q, q, 2);
+        if (cx == 0 || (cx < 0) != HI) continue;
+        const int r = lat_opp(Q, q), m = lat_find(Q, -cx, cy, cz);
+        const F2 s2 = sym ? ft[m] : ft[r];
+        const float v = __shfl_sync(0xffffffffu, second ? lane1(s2) : lane0(s2), src);
+        if (slot == n) {
+            mine = v;
+            p = static_cast<T*>(a.fout_q[q]) + (ip - (cx + cy * a.px + cz * a.pxy));
+        }
+        n++;
+    }
+    if (slot >= n) return;
+    if (!HI || a.nx % A == 0) {
+        uint32_t w32;
+        if constexpr (sizeof(T) == 4) w32 = __float_as_uint(mine);
+        else w32 = held_pack(T{}, mine, mine);
+        uint4* sec = reinterpret_cast<uint4*>(HI ? p : p - (A - 1));
+        sec[half] = make_uint4(w32, w32, w32, w32);
+    } else if (half == 0) {
+        Codec<S>::store_held(p, mine);
+    }
+}
+
+// XM 2: the ghost slots of the x-face cells among a warp's pairs (xf: xface_bits of the lane's pair,
+// act: its active cells), by every lane of the warp; the row's cells start at padded index prow
+template <int Q, int S>
+__device__ __forceinline__ void xface_push_pairs(const StepArgs& a, const F2 (&ft)[Q], int xf, const bool (&act)[2],
+                                                 int prow)
+{
+    const unsigned lo = __ballot_sync(0xffffffffu, (xf & 1) && act[0]);
+    const unsigned hi = __ballot_sync(0xffffffffu, ((xf & 2) && act[0]) || ((xf & 4) && act[1]));
+    const unsigned hi2 = __ballot_sync(0xffffffffu, (xf & 4) && act[1]);
+    if (lo) xface_push_warp<Q, S, false>(a, ft, __ffs(lo) - 1, false, prow);
+    if (hi) xface_push_warp<Q, S, true>(a, ft, __ffs(hi) - 1, hi2 != 0, prow + a.nx - 1);
 }
 
 // the Q pulls of two adjacent cells at ip0 (even), read when any is set, with L2 policy pol; BORDER:
@@ -915,19 +982,25 @@ __device__ __forceinline__ void bulk_pair_adj_eager(const StepArgs& a, int i0, i
     const PairSide side = pair_side<LES>(a, fl, ic);
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
     const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act, i0, i0 + 1, j, k));
-    if (!(act[0] || act[1])) return;
-    const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
-    bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain, &side);
-    // the ghost slots first: the populations are all live until the row stores anyway
-    if constexpr (XM == 2) {
-        if (xf != 0) {  // one or two lanes of the row's first and last warp
-            if ((xf & 1) && act[0]) xface_push<Q, S, 0>(a, ft, false, prow + i0);
-            if ((xf & 2) && act[0]) xface_push<Q, S, 0>(a, ft, true, prow + i0);
-            if ((xf & 4) && act[1]) xface_push<Q, S, 1>(a, ft, true, prow + i0 + 1);
-        }
+    // XM 2 D3Q27 writes the ghost slots with the whole warp: every lane stays
+    constexpr bool WARP_PUSH = XM == 2 && Q == 27;
+    if constexpr (!WARP_PUSH) {
+        if (!(act[0] || act[1])) return;
     }
-    if (hint) pair_adj_store<S, true, Q>(a, ft, act, prow + i0, pol);
-    else pair_adj_store<S, false, Q>(a, ft, act, prow + i0, 0);
+    const int ci[2] = {i0, i0 + 1}, cj[2] = {j, j}, ck[2] = {k, k};
+    const bool any = WARP_PUSH ? (act[0] || act[1]) : true;
+    if (any) bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain, &side);
+    // the ghost slots of the x-face cells of the row's first and last warp, before the row stores (the
+    // populations are live until then anyway)
+    if constexpr (WARP_PUSH) {
+        if (__any_sync(0xffffffffu, xf != 0)) xface_push_pairs<Q, S>(a, ft, xf, act, prow);
+    } else if constexpr (XM == 2) {
+        if (xf != 0) xface_push_lane<Q, S>(a, ft, xf, act, prow + i0, prow + i0 + 1);
+    }
+    if (any) {
+        if (hint) pair_adj_store<S, true, Q>(a, ft, act, prow + i0, pol);
+        else pair_adj_store<S, false, Q>(a, ft, act, prow + i0, 0);
+    }
 }
 
 // bulk_pair (cells i0 and i0 + 32) with the pulls issued together with the flag loads; a cell's
@@ -983,22 +1056,26 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
     const PairSide side = pair_side<LES>(a, fl, ic);
     const bool act[2] = {!(fl[0] & (FL_SOLID | FL_SPECIAL)), !(fl[1] & (FL_SOLID | FL_SPECIAL))};
     const bool plain = __all_sync(0xffffffffu, plain_pair(a, fl, act, i0, i0 + 32, j, k));
-    if (!(act[0] || act[1])) return;
-    const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
-    bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain, &side);
-    // the ghost slots first: the populations are all live until the row stores anyway
-    if constexpr (XM == 2) {
-        if (xf != 0) {  // one lane of the row's first and of its last warp
-            if ((xf & 1) && act[0]) xface_push<Q, S, 0>(a, ft, false, prow + i0);
-            if ((xf & 2) && act[0]) xface_push<Q, S, 0>(a, ft, true, prow + i0);
-            if ((xf & 4) && act[1]) xface_push<Q, S, 1>(a, ft, true, prow + i0 + 32);
-        }
+    constexpr bool WARP_PUSH = XM == 2 && Q == 27;  // as in bulk_pair_adj_eager
+    if constexpr (!WARP_PUSH) {
+        if (!(act[0] || act[1])) return;
     }
+    const int ci[2] = {i0, i0 + 32}, cj[2] = {j, j}, ck[2] = {k, k};
+    const bool any = WARP_PUSH ? (act[0] || act[1]) : true;
+    if (any) bulk_collide2<S, LES, Q>(a, ft, fl, act, ci, cj, ck, ic, plain, &side);
+    // the ghost slots of the x-face cells of the row's first and last warp, as in bulk_pair_adj_eager
+    if constexpr (WARP_PUSH) {
+        if (__any_sync(0xffffffffu, xf != 0)) xface_push_pairs<Q, S>(a, ft, xf, act, prow);
+    } else if constexpr (XM == 2) {
+        if (xf != 0) xface_push_lane<Q, S>(a, ft, xf, act, prow + i0, prow + i0 + 32);
+    }
+    if (any) {
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-        T* p = static_cast<T*>(a.fout_q[q]) + prow + i0;
-        if (act[0]) Codec<S>::store_held(p, lane0(ft[q]));
-        if (act[1]) Codec<S>::store_held(p + 32, lane1(ft[q]));
+        for (int q = 0; q < Q; q++) {
+            T* p = static_cast<T*>(a.fout_q[q]) + prow + i0;
+            if (act[0]) Codec<S>::store_held(p, lane0(ft[q]));
+            if (act[1]) Codec<S>::store_held(p + 32, lane1(ft[q]));
+        }
     }
 }
 
