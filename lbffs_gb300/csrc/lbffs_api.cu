@@ -775,10 +775,12 @@ extern "C" int lbffs_step(lbffs_ctx* c, const lbffs_step_params* p, int nsteps)
         CK(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming));
     }
     // pulls across the grid's border: straight from where the face streaming takes them when the faces
-    // allow it (pull_ok: the x-face cells are boundary-kernel cells), nothing changes the produced
-    // populations after the step (no IBM forcing pass) and the bulk kernel is the per-thread one;
-    // otherwise from the ghost layer, filled before every step
-    const bool pulls = c->pull_ok && c->pulls_on && c->n_markers <= 1 && c->bulk_kind == 0;
+    // allow it (pull_ok) and the bulk kernel is the per-thread one; otherwise from the ghost layer,
+    // filled before every step.  The IBM forcing pass changes populations after the step: the pulls
+    // of modes 1 and 2 read them where the pass left them, as the ghost fill does, but the x-face
+    // cells of mode 3 would have written their ghost slots before it, so with markers mode 3 gives
+    // way to the ghost fill.
+    const bool pulls = c->pull_ok && c->pulls_on && c->bulk_kind == 0 && (c->n_markers <= 1 || c->pull_mode != 3);
     const int pull_mode = pulls ? c->pull_mode : 0;
     for (int s = 0; s < nsteps; s++) {
         StepArgs a;

@@ -18,13 +18,14 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def run_gpu(name, storage="fp32", steps=None, store_fields=2, c=None, run=None, special_kernel=-1):
+def run_gpu(name, storage="fp32", steps=None, store_fields=2, c=None, run=None, special_kernel=-1, border_pulls=1):
     import lbffs_gb300 as L
     if c is None:
         c, run = build(name)
     lat = L.Lattice(c.nx, c.ny, c.nz, q=c.q, storage=storage, collision=run["collision"], sgs=run["sgs"],
                     wall=run["wall"], damping=run.get("damping", "wall"))
     lat.set_special_kernel(special_kernel)
+    lat.set_border_pulls(border_pulls)
     lat.load_case(c)
     if "markers" in run:
         lat.set_markers(run["markers"])
