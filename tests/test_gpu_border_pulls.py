@@ -176,9 +176,11 @@ def test_ghost_slots_follow_state_changes(cuda_lib, storage, q):
         assert np.array_equal(x, y), (k, float(np.abs(x - y).max()))
 
 
+@pytest.mark.parametrize("q", [19, 27])
 @pytest.mark.parametrize("kind,nx,nz,storage", [("channel", 40, 6, "fp32"), ("channel", 40, 6, "fp16s"),
-                                                ("periodic_x", 44, 6, "fp32"), ("cavity", 36, 6, "fp32")])
-def test_pull_modes_with_ibm_forcing_agree_bitwise(cuda_lib, kind, nx, nz, storage):
+                                                ("periodic_x", 44, 6, "fp32"), ("cavity", 36, 6, "fp32"),
+                                                ("cavity", 36, 6, "bf16s")])
+def test_pull_modes_with_ibm_forcing_agree_bitwise(cuda_lib, q, kind, nx, nz, storage):
     """The IBM forcing pass changes populations after the step.  Reading across the border where the
     face streaming takes each population (inlet / outlet or Cyclic x faces) sees them as the ghost fill
     does: bitwise the ghost-layer run, with no fill.  Where the x-face cells would write their own ghost
@@ -186,11 +188,11 @@ def test_pull_modes_with_ibm_forcing_agree_bitwise(cuda_lib, kind, nx, nz, stora
     layer before every step."""
     import lbffs_gb300 as L
     from lbffs_gb300.geometry import cylinder_markers
-    c = _mode_case(19, kind, nx, nz)
+    c = _mode_case(q, kind, nx, nz)
     markers = cylinder_markers(24, nx * 0.4, 6.0, nz / 2.0, 2.5)
     out, halos = [], []
     for on in (1, 0):
-        lat = L.Lattice(c.nx, c.ny, c.nz, q=19, storage=storage)
+        lat = L.Lattice(c.nx, c.ny, c.nz, q=q, storage=storage)
         lat.set_border_pulls(on)
         lat.set_timing(True)
         lat.load_case(c)
