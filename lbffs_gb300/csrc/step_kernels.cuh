@@ -261,7 +261,7 @@ __device__ __forceinline__ long long upwind(int q, const int (&x)[3], const int 
     return ((long long)n[2] * N[1] + n[1]) * N[0] + n[0];
 }
 
-// ---- border pulls (StepArgs::border_pulls 1): the face streaming without a ghost layer ----
+// ---- border pulls (StepArgs::border_pulls 1-3): the face streaming without a ghost fill ----
 // A cell on the grid's border pulls population q from outside the grid when P - c_q lies there.  The
 // reference's face streaming (upwindID_B + reflectOrMirrorQ, D3Q19 kernel.cl:114-575, D3Q27
 // kernel.cl:1133-1146) then takes P's own previous value of missing_dir(q) when a crossed face of P
@@ -1081,10 +1081,13 @@ __device__ __forceinline__ void bulk_pair_eager(const StepArgs& a, int i0, int j
 
 // One thread per BULK_V cells of a row, 32 apart (lane, lane + 32, ...), so each load and store
 // instruction of a warp covers 32 consecutive cells.  Every population is pulled from the same
-// offset for every cell: cells on the domain border read the ghost layer, which k_halo filled
-// with the reference's face streaming at the start of the step.
+// offset for every cell: cells on the domain border read the ghost layer (filled by k_halo with the
+// reference's face streaming before the step, or, for the x-face slots of XM 2, by the x-face cells
+// in the previous step), except where border pulls read across the border directly (rows on a y / z
+// face, and the x-face cells of XM 1).
 // One CTA tile: BULK_BX * bulk_v<Q>() cells of row (j, k) starting at x-block xb.  PF: the tile is
-// CTA (xb, j, k) of a k_bulk grid, so the L2 prefetch of the tiles launched later may run.
+// CTA (xb, j, k) of a k_bulk grid, so the L2 prefetch of the tiles launched later may run.  XM: the
+// kernel's x-face handling (k_bulk).
 template <int Q, int S, int COLL, int SGS, bool LES, bool PF = true, int XM = 0>
 __device__ __forceinline__ void bulk_block(const StepArgs& a, int xb, int j, int k)
 {
