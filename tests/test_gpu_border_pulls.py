@@ -1,14 +1,16 @@
-"""The face streaming of every face kind against the FP32 oracle, cell by cell, in both pull modes.
+"""The face streaming of every face kind against the FP32 oracle, cell by cell, and the border-pull
+modes against the ghost fill, bit for bit.
 
 A border cell pulls across the grid's edge what the reference's face streaming gives it (upwindID_B +
 reflectOrMirrorQ, D3Q19 kernel.cl:114-575, D3Q27 kernel.cl:1133-1146): the periodic image across a
-Cyclic face, the cell's own missing direction across a wall.  A lattice whose two x faces are
-boundary-kernel faces (inlet / outlet) reads those values where they lie (border pulls: bulk rows on a
-y / z face cross it by the row's border); any other lattice reads them from the ghost layer filled
-before each step.  These cases put bulk cells on every face kind the bulk kernels keep (Cyclic,
-BounceBack, Symmetry), with rows wider than one warp (a thread's two cells 32 apart, or adjacent for
-2-byte storage, meet an x face in either lane) and a seeded perturbation of every population so that
-each pull is seen in the result.
+Cyclic face, the cell's own missing direction across a wall.  Where every face carries one code per
+axis the step reads those values where they lie (mode 1: inlet / outlet x faces; mode 2: bulk cells
+pull across Cyclic x faces from per-context plane bases; mode 3: bulk cells on x faces without a
+Cyclic code write the ghost slots they pull from next step themselves); otherwise, and with
+lbffs_set_border_pulls(ctx, 0), from the ghost layer filled before each step.  These cases put bulk
+cells on every face kind the bulk kernels keep (Cyclic, BounceBack, Symmetry), with rows wider than
+one warp (a thread's two cells 32 apart, or adjacent for 2-byte storage, meet an x face in either
+lane) and a seeded perturbation of every population so that each pull is seen in the result.
 Tolerances: FP32 storage within 1e-5 of the largest population (the parity bar of the other cases);
 FP16S storage within 2e-5 absolute (its rounding of the 2^15-scaled deviation is about 1e-6 here).
 """
