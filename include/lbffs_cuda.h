@@ -203,11 +203,14 @@ int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
 int lbffs_set_special_kernel(lbffs_ctx* ctx, int kind);
 
 /* No counterpart in the reference (two ways to the same face streaming, which give identical
-   results).  enabled 1 (the default): where every face carries one boundary code per axis, the
+   results).  enabled 1 (the default): where every face carries one boundary code per axis (and the
+   grid is 3D, unless both x faces are inlet / outlet / fixed-density / wall-function faces), the
    step kernels read each population that crosses the grid's border where the face streaming takes
-   it (the periodic image, or the cell's own value of the bounce-back / mirror direction), and no
-   ghost layer is filled; 0: a ghost-layer fill before every step holds those values, and every
-   cell pulls from a fixed offset. */
+   it (the periodic image, or the cell's own value of the bounce-back / mirror direction) instead of
+   from a ghost layer filled before every step; where bulk cells lie on x faces without a Cyclic
+   code, those cells write the x ghost slots they pull from next step themselves, and the ghost
+   layer is filled once, before the first step after the populations were set from outside a step.
+   0: the ghost-layer fill before every step, every cell pulling from a fixed offset. */
 int lbffs_set_border_pulls(lbffs_ctx* ctx, int enabled);
 
 /* setSolid + setNeiSolid (src/walls.hpp:159-216) on the device, bit for bit the reference's host
