@@ -203,8 +203,9 @@ int lbffs_set_bulk_kernel(lbffs_ctx* ctx, int kind);
 int lbffs_set_special_kernel(lbffs_ctx* ctx, int kind);
 
 /* No counterpart in the reference (two ways to the same face streaming, which give identical
-   results).  enabled 1 (the default): where every face carries one boundary code per axis (and the
-   grid is 3D, unless both x faces are inlet / outlet / fixed-density / wall-function faces), the
+   results).  enabled 1 (the default): where every face carries one boundary code per axis (on a 2D
+   grid: and the z faces carry no wall code, or both x faces are inlet / outlet / fixed-density /
+   wall-function faces), the
    step kernels read each population that crosses the grid's border where the face streaming takes
    it (the periodic image, or the cell's own value of the bounce-back / mirror direction) instead of
    from a ghost layer filled before every step; where bulk cells lie on x faces without a Cyclic

@@ -397,17 +397,20 @@ static int commit(lbffs_ctx* c)
         // mode 1: both x faces are boundary-kernel faces and the bulk kernels cross only y / z faces;
         // modes 3 and 2: x-face bulk cells take their x-crossing pulls through ghost slots they write
         // themselves (no Cyclic x face: the value is the cell's own) or from per-context plane bases
-        // (where that kernel is built).  A 2D grid keeps the ghost layer: its x-face cells are face
-        // cells for the z-crossing directions where their row neighbours are not.
+        // (where that kernel is built).  A 2D grid with a wall code on its z faces keeps the ghost
+        // layer: there its x-face cells are face cells for the z-crossing directions where their row
+        // neighbours are not, so a pair's shared c_x = 0 pull would not hold; with Cyclic (or outlet)
+        // z codes every cell of a row takes those directions alike.
         auto kernel_face = [](int code) {
             return code == BC_OUTLET || code == BC_FIXVEL || code == BC_FIXDEN || code == BC_WALLFN;
         };
         const bool x_kernel = kernel_face(c->face_codes & 7) && kernel_face((c->face_codes >> 3) & 7);
         const bool x_cyclic = (c->face_codes & 7) == BC_CYCLIC || ((c->face_codes >> 3) & 7) == BC_CYCLIC;
         const bool x_pulls = xface_pulls_built(c->Q, c->d.storage == LBFFS_FP32 ? ST_FP32 : ST_FP16S);
+        const bool z_wall = is_wall_code((c->face_codes >> 12) & 7) || is_wall_code((c->face_codes >> 15) & 7);
         c->pull_mode = !(LBFFS_BORDER_PULLS && c->face_ok) ? 0
                        : x_kernel                            ? 1
-                       : nz <= 1                             ? 0
+                       : nz <= 1 && z_wall                   ? 0
                        : !x_cyclic                           ? 3
                        : x_pulls                             ? 2
                                                              : 0;

@@ -103,11 +103,10 @@ def _expected_halos(kind, q, storage, nz, steps):
     """Ghost fills a run of `steps` steps launches: none where the lattice pulls across all its faces
     (inlet / outlet x faces; Cyclic x faces where that kernel is built), one where the x-face cells
     write their own ghost slots (x faces without a Cyclic code: the fill before the first step), one
-    per step otherwise (a 2D grid; D3Q27 2-byte storage with Cyclic x faces)."""
+    per step otherwise (D3Q27 2-byte storage with Cyclic x faces; a 2D grid with wall-coded z faces,
+    which these cases do not have: their 2D grids leave the z faces Cyclic)."""
     if kind == "channel":
         return 0
-    if nz == 1:
-        return steps
     if kind == "periodic_x":
         return 0 if (q == 19 or storage == "fp32") else steps
     return 1
@@ -126,7 +125,7 @@ def test_pull_modes_agree_bitwise(cuda_lib, storage, q, collision, sgs, les, kin
     fields after 5 steps.  Bulk cells lie on the x faces here (cavity, walls, symmetry, periodic x;
     odd row lengths and a second row tile end on an x face in either cell of a pair), beside
     boundary-kernel cells (the solid blocks' links, the lid), or only boundary-kernel cells do (the
-    channel's inlet and outlet).  A 2D grid keeps the ghost layer in both settings."""
+    channel's inlet and outlet); the 2D grid has Cyclic z faces."""
     import lbffs_gb300 as L
     c = _mode_case(q, kind, nx, nz)
     out, halos = [], []
